@@ -1,0 +1,158 @@
+/*
+ * gpb.h -- C ABI of libgpb, a GB300 (sm_103a) implementation of the gPb
+ * contour stage of yanyp/UCM-MPI-GPU.
+ *
+ * It replaces the reference's engine boundary
+ *     void computeGPb(unsigned rank, unsigned width, unsigned height,
+ *                     unsigned* data, float** hostGPb, float** hostGPbAllConcat);
+ *     int  getCudaDeviceCount();
+ * (damascene/include/globalPb.h:35,44; called from src/globalPb.cpp:282 inside
+ * GlobalPbCuda, src/globalPb.cpp:247-313).  Those two C++ symbols are also
+ * exported with their original signatures and semantics (see gpb_damascene.h).
+ *
+ * Conventions
+ *  - Input pixels are packed as data[y*width + x] = B<<16 | G<<8 | R
+ *    (src/globalPb.cpp:264-276).
+ *  - Every entry point returns a gpb_status and never throws.
+ *  - A context owns its device buffers, stream and tables; it is reentrant per
+ *    context and may be used from one host thread at a time.
+ *  - Output buffers returned through float** are malloc()ed; release them with
+ *    free() or gpb_free(), as the reference's caller does (src/globalPb.cpp:310).
+ */
+#ifndef GPB_H_
+#define GPB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GPB_OK = 0,
+  GPB_ERR_ARG = 1,       /* bad argument (size, NULL pointer, missing codebook) */
+  GPB_ERR_CUDA = 2,      /* a CUDA runtime call failed                           */
+  GPB_ERR_NOMEM = 3,     /* device or host allocation failed                     */
+  GPB_ERR_NOCONV = 4,    /* the eigensolver hit its matvec cap                   */
+  GPB_ERR_TIMEOUT = 5,   /* a bounded device wait gave up                        */
+  GPB_ERR_INTERNAL = 6
+} gpb_status;
+
+typedef enum {
+  /* gPb of the reference's CPU path (src/globalPb.cpp:128-245, fixes on):
+   * orient planes [o][y][x] row-major, o = 0..7; nmax = max_o |gPb_o|. */
+  GPB_COMPAT_CPU = 0,
+  /* computeGPb output (damascene/src/damascene.cu:546-603): GPU weight sets,
+   * nmax = max_o gPb_o where mPb > 0.05 (before the sigmoid), orient planes
+   * sigmoid-rescaled, plane i = orientation {4,5,6,7,0,1,2,3}[i], each stored
+   * column-major ([i*H*W + x*H + y]). */
+  GPB_COMPAT_DAMASCENE = 1
+} gpb_compat;
+
+typedef enum {
+  GPB_EIG_LANCZOS = 0,   /* plain cold-start thick-restart Lanczos (Krylov-Schur) */
+  GPB_EIG_WARM = 1       /* warm-started block solver, Lanczos as fallback         */
+} gpb_eig_mode;
+
+typedef struct {
+  int device;            /* CUDA device ordinal, -1 = current                     */
+  int compat;            /* gpb_compat                                            */
+  int nvec;              /* eigenvectors, including the trivial one (9)           */
+  float eig_tol;         /* Ritz residual tolerance on the unit eigenvectors      */
+  int eig_max_matvecs;   /* cap per patch                                         */
+  int krylov_dim;        /* Krylov-Schur basis size m                             */
+  int krylov_keep;       /* vectors kept at a restart                             */
+  int eig_mode;          /* gpb_eig_mode                                          */
+  int keep_intermediates;/* 1: retain per-stage buffers for gpb_fetch(); 2: also counts */
+} gpb_params;
+
+typedef struct gpb_ctx gpb_ctx;
+
+/* one patch of a batch: a window of a packed image (row stride in pixels) */
+typedef struct {
+  uint32_t width, height;
+  const uint32_t* packed_bgr;
+  size_t stride;
+} gpb_patch;
+
+/* per-patch outputs; NULL members are malloc()ed by the library */
+typedef struct {
+  float* nmax;    /* H*W                  */
+  float* orient;  /* 8*H*W (layout per compat) */
+} gpb_result;
+
+typedef struct {
+  double ms_total, ms_h2d, ms_texton, ms_cues, ms_nms, ms_buildw, ms_eig, ms_spb, ms_d2h;
+  long matvecs_max;           /* largest per-patch matvec count of the last call   */
+  long matvecs_total;
+  int restarts;
+  float max_residual;         /* largest final Ritz residual                       */
+  long texton_repaired;       /* pixels whose texton label went to the FP64 repair */
+  int gpu_launches;           /* kernels launched by the last call                 */
+  /* per-kernel timing of the eigensolver (filled when GPB_PROFILE=1 in the
+   * environment at gpb_create): total ms, launches and algorithmic bytes */
+  double spmv_ms, orth_ms;
+  long spmv_launches, orth_launches;
+  double spmv_bytes, orth_bytes;
+} gpb_stats;
+
+/* intermediates available through gpb_fetch() (keep_intermediates = 1) */
+typedef enum {
+  GPB_STAGE_TEXTON = 0,   /* uint8  H*W                              */
+  GPB_STAGE_LABBINS = 1,  /* uint8  3*H*W (L, a, b bins)              */
+  GPB_STAGE_MPB_O = 2,    /* float  8*H*W weighted cue sum per orient */
+  GPB_STAGE_MPB = 3,      /* float  H*W   mPb after NMS and clip      */
+  GPB_STAGE_W = 4,        /* float  H*W*81 symmetric affinities       */
+  GPB_STAGE_EVALS = 5,    /* float  nvec                               */
+  GPB_STAGE_EVECS = 6,    /* float  nvec*H*W unit eigvecs of A        */
+  GPB_STAGE_SPB = 7,      /* float  8*H*W                              */
+  GPB_STAGE_CUES = 8,     /* float  12*8*H*W raw cue maps             */
+  GPB_STAGE_GPB_O = 9,    /* float  8*H*W gPb planes before layout    */
+  /* uint8 H*W*4*4*32*32, keep_intermediates = 2: per pixel, annulus
+   * (r <= 3, 5, 10, 20, cumulative), cue (L, a, b, texton), counter row
+   * (half*16 + slice) and bin -- the raw half-disc histogram counts
+   * (sum the two halves of a slice) */
+  GPB_STAGE_COUNTS = 10
+} gpb_stage;
+
+void gpb_default_params(gpb_params* p);
+gpb_status gpb_create(gpb_ctx** ctx, const gpb_params* p);
+void gpb_destroy(gpb_ctx* ctx);
+
+/* The 13 x K FP32 texton codebook (row f = Schmid filter f, column k =
+ * codeword k), as src/SPFeatures.cpp:300-313 reads from
+ * <piece>_texton_codebook.yml.  K <= 32. */
+gpb_status gpb_set_codebook(gpb_ctx* ctx, const float* codebook, int K);
+/* Same, parsed from an OpenCV YAML file holding "texton_codebook". */
+gpb_status gpb_load_codebook_yml(gpb_ctx* ctx, const char* path);
+
+/* One patch; *out_nmax (H*W) and *out_orient (8*H*W) are malloc()ed. */
+gpb_status gpb_compute(gpb_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* packed_bgr,
+                       float** out_nmax, float** out_orient);
+
+/* n patches of any sizes (each side >= 32) in one batched pass. */
+gpb_status gpb_compute_batch(gpb_ctx* ctx, const gpb_patch* patches, size_t n, gpb_result* out);
+
+/* Device-resident variant: d_packed holds the patches back to back (patch i
+ * at d_packed + offsets[i], tightly packed rows); results are written to
+ * d_nmax / d_orient at the same offsets (orient: 8 planes per patch starting
+ * at 8*offsets[i]).  Host arrays widths/heights/offsets have n entries. */
+gpb_status gpb_compute_batch_device(gpb_ctx* ctx, size_t n, const uint32_t* widths,
+                                    const uint32_t* heights, const size_t* offsets,
+                                    const uint32_t* d_packed, float* d_nmax, float* d_orient);
+
+/* Copy an intermediate of patch `patch` of the last call into dst. */
+gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst, size_t dst_bytes);
+
+gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st);
+
+int gpb_device_count(void);
+const char* gpb_status_str(gpb_status s);
+void gpb_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPB_H_ */

@@ -251,14 +251,17 @@ void orc_mirror_u8(const uint8_t* src, int H, int W, int b, uint8_t* dst) {
 /* orientation_slice_map, lib_image.cc:3052-3081, evaluated at the window
  * position that compute_hist_gradient_2D (lib_image.cc:3120-3235, a
  * convolution) pairs with the label at offset (drow, dcol) from the centre:
- * window index (r-drow, r-dcol), i.e. the point (-drow-0.5, -dcol-0.5). */
+ * window index (r-drow, r-dcol), i.e. the point (-drow-0.5, -dcol-0.5).  The
+ * reference mixes double and long double in this expression; as compiled
+ * (x86-64, -O2) its map equals floor((atan2(y,x) + pi) / pi * 8) in double
+ * at every offset within radius 20, the exact diagonals included (checked
+ * against the compiled reference cores), which is what this evaluates. */
 int orc_slice_index(int r, int drow, int dcol) {
   (void)r;
   const double x = -(double)drow - 0.5, y = -(double)dcol - 0.5;
-  const long double ori = (long double)atan2(y, x) + PI_L;
-  unsigned long idx = (unsigned long)floorl(ori / PI_L * (long double)8.0);
-  if (idx >= 16) idx = 15;
-  return (int)idx;
+  int idx = (int)floor((atan2(y, x) + M_PI) / M_PI * 8.0);
+  if (idx > 15) idx = 15;
+  return idx;
 }
 
 /* lib_image::gaussian(sigma, 0, false) (lib_image.cc:1374-1441): support

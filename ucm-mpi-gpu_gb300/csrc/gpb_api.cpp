@@ -1,0 +1,890 @@
+// gpb_api.cpp -- the C ABI of libgpb (include/gpb.h): context, batch layout,
+// the per-batch pipeline and the eigensolver drivers.
+//
+// Pipeline per batch, on one stream:
+//   H2D -> convert -> texton (+ FP64 repair) -> max label -> local cues ->
+//   NMS -> buildW -> degree/scale -> eigensolver -> min/max -> sPb/gPb -> D2H
+// It replaces computeGPb (damascene/src/damascene.cu:249-661): same inputs
+// and, in GPB_COMPAT_DAMASCENE, the same output layout.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/gpb.h"
+#include "gpb_internal.h"
+#include "k_eig.h"
+#include "kernels.h"
+
+namespace gpb {
+void sym_eig(double* A, int n, double* w, double* Z);
+}
+
+using namespace gpb;
+
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t e_ = (x);                       \
+    if (e_ != cudaSuccess) {                    \
+      ctx->last_error = cudaGetErrorString(e_); \
+      return GPB_ERR_CUDA;                      \
+    }                                           \
+  } while (0)
+
+template <class T>
+static cudaError_t grow(T*& p, size_t& cap, size_t need) {
+  if (need <= cap && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc((void**)&p, need * sizeof(T) + 256);
+  if (e != cudaSuccess) return e;
+  cap = need;
+  return cudaMemset(p, 0, need * sizeof(T) + 256);
+}
+
+struct Buf {
+  // image-level
+  uint32_t* packed = nullptr; size_t c_packed = 0;
+  uint8_t* grey = nullptr; size_t c_grey = 0;
+  uint32_t* lab4 = nullptr; size_t c_lab4 = 0;
+  int* nbins = nullptr; size_t c_nbins = 0;
+  int* repair = nullptr; size_t c_repair = 0;
+  int* repair_count = nullptr; size_t c_rc = 0;
+  float* mpbo = nullptr; size_t c_mpbo = 0;
+  float* go = nullptr; size_t c_go = 0;
+  float* mpb = nullptr; size_t c_mpb = 0;
+  float* raw = nullptr; size_t c_raw = 0;
+  float* wfull = nullptr; size_t c_wfull = 0;
+  uint8_t* counts = nullptr; size_t c_counts = 0;
+  // padded vector layout
+  float* wup = nullptr; size_t c_wup = 0;
+  float* aup = nullptr; size_t c_aup = 0;
+  float* deg = nullptr; size_t c_deg = 0;
+  float* dis = nullptr; size_t c_dis = 0;
+  float* adiag = nullptr; size_t c_adiag = 0;
+  float* V[2] = {nullptr, nullptr}; size_t c_V[2] = {0, 0};
+  float* W[2] = {nullptr, nullptr}; size_t c_W[2] = {0, 0};
+  float* evec = nullptr; size_t c_evec = 0;
+  // solver state
+  double* part = nullptr; size_t c_part = 0;
+  double* hbuf = nullptr; size_t c_hbuf = 0;
+  double* T = nullptr; size_t c_T = 0;
+  double* Y = nullptr; size_t c_Y = 0;
+  double* beta2 = nullptr; size_t c_beta2 = 0;
+  int* counter = nullptr; size_t c_counter = 0;
+  int* active = nullptr; size_t c_active = 0;
+  int* decision = nullptr; size_t c_decision = 0;
+  int* nkeep = nullptr; size_t c_nkeep = 0;
+  float* evals = nullptr; size_t c_evals = 0;
+  float* mm = nullptr; size_t c_mm = 0;
+  float* spb = nullptr; size_t c_spb = 0;
+  float* gpbo = nullptr; size_t c_gpbo = 0;
+  // outputs
+  float* nmax = nullptr; size_t c_nmax = 0;
+  float* orient = nullptr; size_t c_orient = 0;
+  // tables
+  PatchDev* patches = nullptr; size_t c_patches = 0;
+  int4* work_tex = nullptr; size_t c_wt = 0;
+  int4* work_cue = nullptr; size_t c_wc = 0;
+  int4* work16 = nullptr; size_t c_w16 = 0;
+  EigTile* tiles = nullptr; size_t c_tiles = 0;
+  int* tile_begin = nullptr; size_t c_tb = 0;
+  int* tile_count = nullptr; size_t c_tc = 0;
+};
+
+struct gpb_ctx {
+  gpb_params prm;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  HostTables tab;
+  IcPath* d_ic = nullptr;
+  double* d_k32_ring = nullptr;
+  int* d_ring_of = nullptr;
+  int K = 0;
+  Buf b;
+  std::string last_error;
+  // last call
+  std::vector<PatchDev> patches;
+  long long total_pix = 0, lvec = 0;
+  std::string layout_key;
+  std::vector<float> evals_host;  // npatch * nvec
+  gpb_stats stats;
+  int launches = 0;
+  // pinned staging
+  uint32_t* h_packed = nullptr; size_t c_hpacked = 0;
+  float* h_out = nullptr; size_t c_hout = 0;
+  cudaEvent_t ev[12];
+  // optional per-kernel timing of the eigensolver launches
+  bool profile = false;
+  std::vector<cudaEvent_t> pev;
+  std::vector<int> pkind;      // 0 spmv, 1 orth
+  std::vector<double> pbytes;  // algorithmic bytes of that launch
+  size_t pn = 0;
+};
+
+// events around one eigensolver launch (kind 0 = SpMV, 1 = CGS pass)
+static void prof_begin(gpb_ctx* ctx, int kind, double bytes) {
+  if (!ctx->profile) return;
+  if (ctx->pn + 2 > ctx->pev.size()) {
+    for (int i = 0; i < 256; i++) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ctx->pev.push_back(e);
+    }
+    ctx->pkind.resize(ctx->pev.size());
+    ctx->pbytes.resize(ctx->pev.size());
+  }
+  ctx->pkind[ctx->pn] = kind;
+  ctx->pbytes[ctx->pn] = bytes;
+  cudaEventRecord(ctx->pev[ctx->pn++], ctx->st);
+}
+static void prof_end(gpb_ctx* ctx) {
+  if (!ctx->profile) return;
+  cudaEventRecord(ctx->pev[ctx->pn++], ctx->st);
+}
+static void prof_collect(gpb_ctx* ctx) {
+  if (!ctx->profile) return;
+  cudaStreamSynchronize(ctx->st);
+  for (size_t i = 0; i + 1 < ctx->pn; i += 2) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->pev[i], ctx->pev[i + 1]);
+    if (ctx->pkind[i] == 0) {
+      ctx->stats.spmv_ms += ms;
+      ctx->stats.spmv_launches++;
+      ctx->stats.spmv_bytes += ctx->pbytes[i];
+    } else {
+      ctx->stats.orth_ms += ms;
+      ctx->stats.orth_launches++;
+      ctx->stats.orth_bytes += ctx->pbytes[i];
+    }
+  }
+  ctx->pn = 0;
+}
+
+extern "C" void gpb_default_params(gpb_params* p) {
+  p->device = -1;
+  p->compat = GPB_COMPAT_CPU;
+  p->nvec = 9;
+  p->eig_tol = 3e-6f;
+  p->eig_max_matvecs = 20000;
+  p->krylov_dim = 40;
+  p->krylov_keep = 26;
+  p->eig_mode = GPB_EIG_LANCZOS;
+  p->keep_intermediates = 0;
+}
+
+extern "C" const char* gpb_status_str(gpb_status s) {
+  switch (s) {
+    case GPB_OK: return "ok";
+    case GPB_ERR_ARG: return "invalid argument";
+    case GPB_ERR_CUDA: return "CUDA error";
+    case GPB_ERR_NOMEM: return "out of memory";
+    case GPB_ERR_NOCONV: return "eigensolver did not converge";
+    case GPB_ERR_TIMEOUT: return "device wait timed out";
+    default: return "internal error";
+  }
+}
+
+extern "C" void gpb_free(void* p) { free(p); }
+
+extern "C" int gpb_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
+  if (!out) return GPB_ERR_ARG;
+  *out = nullptr;
+  gpb_ctx* ctx = new (std::nothrow) gpb_ctx();
+  if (!ctx) return GPB_ERR_NOMEM;
+  if (p) ctx->prm = *p;
+  else gpb_default_params(&ctx->prm);
+  gpb_params& q = ctx->prm;
+  if (q.nvec < 2 || q.nvec > kMaxNvec || q.krylov_dim > kMaxKrylov || q.krylov_keep >= q.krylov_dim ||
+      q.krylov_keep < q.nvec || !(q.eig_tol > 0)) {
+    delete ctx;
+    return GPB_ERR_ARG;
+  }
+  if (q.device >= 0) {
+    if (cudaSetDevice(q.device) != cudaSuccess) {
+      delete ctx;
+      return GPB_ERR_CUDA;
+    }
+  }
+  cudaGetDevice(&ctx->device);
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return GPB_ERR_CUDA;
+  }
+  for (int i = 0; i < 12; i++) cudaEventCreate(&ctx->ev[i]);
+  {
+    const char* pe = getenv("GPB_PROFILE");
+    ctx->profile = pe && pe[0] == '1';
+  }
+  build_tables(ctx->tab, q.compat);
+  cudaStream_t s = ctx->st;
+  upload_front(ctx->tab, s);
+  upload_cues(ctx->tab, s);
+  upload_buildw(ctx->tab, s);
+  upload_eig(ctx->tab, s);
+  upload_spb(ctx->tab, s);
+  // global tables: IC paths, FP64 ring coefficients and the offset->ring map
+  size_t nic = ctx->tab.ic.size();
+  std::vector<int> ring_of(2401);
+  {
+    int rid[2 * 24 * 24 + 1];
+    for (int t = 0; t <= 2 * 24 * 24; t++) rid[t] = -1;
+    for (int a = 0; a <= 24; a++)
+      for (int bb = 0; bb <= 24; bb++) rid[a * a + bb * bb] = 0;
+    int nr = 0;
+    for (int t = 0; t <= 2 * 24 * 24; t++)
+      if (rid[t] == 0) rid[t] = nr++;
+    for (int o = 0; o < 2401; o++) {
+      const int dy = o / 49 - 24, dx = o % 49 - 24;
+      ring_of[o] = rid[dy * dy + dx * dx];
+    }
+  }
+  if (cudaMalloc(&ctx->d_ic, nic * sizeof(IcPath)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_k32_ring, ctx->tab.k32_ring.size() * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_ring_of, 2401 * sizeof(int)) != cudaSuccess) {
+    gpb_destroy(ctx);
+    return GPB_ERR_NOMEM;
+  }
+  cudaMemcpyAsync(ctx->d_ic, ctx->tab.ic.data(), nic * sizeof(IcPath), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(ctx->d_k32_ring, ctx->tab.k32_ring.data(), ctx->tab.k32_ring.size() * sizeof(double),
+                  cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(ctx->d_ring_of, ring_of.data(), 2401 * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
+    gpb_destroy(ctx);
+    return GPB_ERR_CUDA;
+  }
+  *out = ctx;
+  return GPB_OK;
+}
+
+extern "C" void gpb_destroy(gpb_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  Buf& b = ctx->b;
+  void* ptrs[] = {b.packed, b.grey, b.lab4, b.nbins, b.repair, b.repair_count, b.mpbo, b.go, b.mpb, b.raw,
+                  b.wfull, b.counts, b.wup, b.aup, b.deg, b.dis, b.adiag, b.V[0], b.V[1], b.W[0], b.W[1], b.evec,
+                  b.part, b.hbuf, b.T, b.Y, b.beta2, b.counter, b.active, b.decision, b.nkeep, b.evals,
+                  b.mm, b.spb, b.gpbo, b.nmax, b.orient, b.patches, b.work_tex, b.work_cue, b.work16,
+                  b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
+  if (ctx->h_out) cudaFreeHost(ctx->h_out);
+  for (int i = 0; i < 12; i++) cudaEventDestroy(ctx->ev[i]);
+  for (cudaEvent_t e : ctx->pev) cudaEventDestroy(e);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+}
+
+extern "C" gpb_status gpb_set_codebook(gpb_ctx* ctx, const float* cb, int K) {
+  if (!ctx || !cb || K < 1 || K > kMaxCodewords) return GPB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  upload_codebook(cb, K, ctx->st);
+  if (cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
+  ctx->K = K;
+  return GPB_OK;
+}
+
+// minimal reader for an OpenCV FileStorage YAML matrix named texton_codebook
+extern "C" gpb_status gpb_load_codebook_yml(gpb_ctx* ctx, const char* path) {
+  if (!ctx || !path) return GPB_ERR_ARG;
+  FILE* f = fopen(path, "rb");
+  if (!f) return GPB_ERR_ARG;
+  std::string s;
+  char buf[4096];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
+  fclose(f);
+  size_t at = s.find("texton_codebook");
+  if (at == std::string::npos) return GPB_ERR_ARG;
+  auto num_after = [&](const char* key, size_t from) -> long {
+    size_t k = s.find(key, from);
+    if (k == std::string::npos) return -1;
+    return strtol(s.c_str() + k + strlen(key), nullptr, 10);
+  };
+  const long rows = num_after("rows:", at), cols = num_after("cols:", at);
+  size_t d = s.find("data:", at);
+  if (rows != kNschmid || cols < 1 || cols > kMaxCodewords || d == std::string::npos) return GPB_ERR_ARG;
+  d = s.find('[', d);
+  if (d == std::string::npos) return GPB_ERR_ARG;
+  std::vector<float> v;
+  const char* c = s.c_str() + d + 1;
+  while ((long)v.size() < rows * cols) {
+    char* e;
+    const double x = strtod(c, &e);
+    if (e == c) {
+      if (*c == 0) break;
+      c++;
+      continue;
+    }
+    v.push_back((float)x);
+    c = e;
+  }
+  if ((long)v.size() != rows * cols) return GPB_ERR_ARG;
+  return gpb_set_codebook(ctx, v.data(), (int)cols);
+}
+
+// ------------------------------------------------------------------ batch
+namespace {
+
+struct Layout {
+  std::vector<PatchDev> patches;
+  std::vector<int4> work_tex, work_cue, work16;
+  std::vector<EigTile> tiles;
+  std::vector<int> tile_begin, tile_count;
+  long long total_pix = 0, lvec = 0;
+  int max_side = 0;
+};
+
+Layout make_layout(size_t n, const uint32_t* ws, const uint32_t* hs) {
+  Layout L;
+  int wmax = 0;
+  for (size_t i = 0; i < n; i++) wmax = std::max(wmax, (int)ws[i]);
+  const long long pad = (((long long)kStencilR * wmax + kStencilR) + 63) / 64 * 64;
+  long long pix = 0, vec = pad;
+  for (size_t i = 0; i < n; i++) {
+    PatchDev P;
+    P.W = (int)ws[i];
+    P.H = (int)hs[i];
+    P.N = P.W * P.H;
+    for (int c = 0; c < 4; c++) P.nb[c] = 0;
+    P.pix = pix;
+    P.vec = vec;
+    pix += ((long long)P.N + 31) / 32 * 32;
+    vec += ((long long)P.N + 31) / 32 * 32 + pad;
+    L.patches.push_back(P);
+    const int pi = (int)i;
+    for (int y = 0; y < P.H; y += 16)
+      for (int x = 0; x < P.W; x += 16) {
+        L.work_tex.push_back(make_int4(pi, y, x, 0));
+        L.work16.push_back(make_int4(pi, y, x, 0));
+      }
+    for (int y = 0; y < P.H; y += kCueTileH)
+      for (int x = 0; x < P.W; x += kCueTileW) L.work_cue.push_back(make_int4(pi, y, x, 0));
+    L.tile_begin.push_back((int)L.tiles.size());
+    for (int p0 = 0; p0 < P.N; p0 += kEigTile) {
+      EigTile t;
+      t.patch = pi;
+      t.p0 = p0;
+      t.p1 = std::min(P.N, p0 + kEigTile);
+      t.pad = 0;
+      L.tiles.push_back(t);
+    }
+    L.tile_count.push_back((int)L.tiles.size() - L.tile_begin.back());
+  }
+  L.total_pix = pix;
+  L.lvec = vec;
+  return L;
+}
+
+}  // namespace
+
+static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_changed) {
+  Buf& b = ctx->b;
+  const gpb_params& q = ctx->prm;
+  const size_t P = L.total_pix, V = L.lvec, np = L.patches.size(), nt = L.tiles.size();
+  const int m = q.krylov_dim;
+  std::vector<cudaError_t> es;
+  es.push_back(grow(b.packed, b.c_packed, P));
+  es.push_back(grow(b.grey, b.c_grey, P));
+  es.push_back(grow(b.lab4, b.c_lab4, P));
+  es.push_back(grow(b.nbins, b.c_nbins, 4 * np));
+  es.push_back(grow(b.repair, b.c_repair, 2 * (P / 4 + 1024)));
+  es.push_back(grow(b.repair_count, b.c_rc, 1));
+  es.push_back(grow(b.mpbo, b.c_mpbo, 8 * P));
+  es.push_back(grow(b.go, b.c_go, 8 * P));
+  es.push_back(grow(b.mpb, b.c_mpb, P));
+  if (q.keep_intermediates) {
+    es.push_back(grow(b.raw, b.c_raw, 96 * P));
+    es.push_back(grow(b.wfull, b.c_wfull, 81 * P));
+    es.push_back(grow(b.spb, b.c_spb, 8 * P));
+    es.push_back(grow(b.gpbo, b.c_gpbo, 8 * P));
+    if (q.keep_intermediates >= 2) es.push_back(grow(b.counts, b.c_counts, (size_t)kNannulus * 4 * 32 * 32 * P));
+  }
+  const size_t old_wup = b.c_wup;
+  es.push_back(grow(b.wup, b.c_wup, (size_t)kUpper * V));
+  es.push_back(grow(b.aup, b.c_aup, (size_t)kUpper * V));
+  es.push_back(grow(b.deg, b.c_deg, V));
+  es.push_back(grow(b.dis, b.c_dis, V));
+  es.push_back(grow(b.adiag, b.c_adiag, V));
+  for (int i = 0; i < 2; i++) {
+    es.push_back(grow(b.V[i], b.c_V[i], (size_t)(m + 1) * V));
+    es.push_back(grow(b.W[i], b.c_W[i], V));
+  }
+  es.push_back(grow(b.evec, b.c_evec, (size_t)q.nvec * V));
+  es.push_back(grow(b.part, b.c_part, nt * kEigWarps * (size_t)(m + 1)));
+  es.push_back(grow(b.hbuf, b.c_hbuf, np * (m + 1)));
+  es.push_back(grow(b.T, b.c_T, np * m * m));
+  es.push_back(grow(b.Y, b.c_Y, np * m * m));
+  es.push_back(grow(b.beta2, b.c_beta2, np));
+  es.push_back(grow(b.counter, b.c_counter, np));
+  es.push_back(grow(b.active, b.c_active, np));
+  es.push_back(grow(b.decision, b.c_decision, np));
+  es.push_back(grow(b.nkeep, b.c_nkeep, np));
+  es.push_back(grow(b.evals, b.c_evals, np * q.nvec));
+  es.push_back(grow(b.mm, b.c_mm, np * q.nvec * 2));
+  es.push_back(grow(b.nmax, b.c_nmax, P));
+  es.push_back(grow(b.orient, b.c_orient, 8 * P));
+  es.push_back(grow(b.patches, b.c_patches, np));
+  es.push_back(grow(b.work_tex, b.c_wt, L.work_tex.size()));
+  es.push_back(grow(b.work_cue, b.c_wc, L.work_cue.size()));
+  es.push_back(grow(b.work16, b.c_w16, L.work16.size()));
+  es.push_back(grow(b.tiles, b.c_tiles, nt));
+  es.push_back(grow(b.tile_begin, b.c_tb, np));
+  es.push_back(grow(b.tile_count, b.c_tc, np));
+  for (cudaError_t e : es)
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? GPB_ERR_NOMEM : GPB_ERR_CUDA;
+  (void)old_wup;
+  if (layout_changed) {
+    // the padded layout relies on zero pads: clear every padded array
+    cudaStream_t s = ctx->st;
+    cudaMemsetAsync(b.wup, 0, (size_t)kUpper * V * sizeof(float), s);
+    cudaMemsetAsync(b.aup, 0, (size_t)kUpper * V * sizeof(float), s);
+    cudaMemsetAsync(b.deg, 0, V * sizeof(float), s);
+    cudaMemsetAsync(b.dis, 0, V * sizeof(float), s);
+    cudaMemsetAsync(b.adiag, 0, V * sizeof(float), s);
+    for (int i = 0; i < 2; i++) {
+      cudaMemsetAsync(b.V[i], 0, (size_t)(m + 1) * V * sizeof(float), s);
+      cudaMemsetAsync(b.W[i], 0, V * sizeof(float), s);
+    }
+    cudaMemsetAsync(b.evec, 0, (size_t)q.nvec * V * sizeof(float), s);
+    cudaMemsetAsync(b.counter, 0, np * sizeof(int), s);
+  }
+  return GPB_OK;
+}
+
+// the Krylov-Schur driver (plain cold-start Lanczos with thick restart)
+static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
+  Buf& b = ctx->b;
+  const gpb_params& q = ctx->prm;
+  cudaStream_t s = ctx->st;
+  const int np = (int)L.patches.size(), nt = (int)L.tiles.size();
+  const int m = q.krylov_dim, keep = q.krylov_keep, nev = q.nvec;
+  EigArgs a;
+  a.patches = b.patches;
+  a.tiles = b.tiles;
+  a.tile_begin = b.tile_begin;
+  a.tile_count = b.tile_count;
+  a.a_up = b.aup;
+  a.a_diag = b.adiag;
+  a.part = b.part;
+  a.hbuf = b.hbuf;
+  a.T = b.T;
+  a.Y = b.Y;
+  a.beta2 = b.beta2;
+  a.counter = b.counter;
+  a.active = b.active;
+  a.decision = b.decision;
+  a.nkeep = b.nkeep;
+  a.lvec = L.lvec;
+  a.m = m;
+  a.mp1 = m + 1;
+  std::vector<int> active(np, 1), decision(np, 0), nkeep(np, 0), mv(np, 0);
+  std::vector<double> T((size_t)np * m * m), Y((size_t)np * m * m), beta2(np);
+  std::vector<float> evals((size_t)np * nev, 0.f);
+  float* Vc = b.V[0];
+  float* Va = b.V[1];
+  float* cur = b.W[0];
+  float* nxt = b.W[1];
+  CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.decision, decision.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(b.T, 0, (size_t)np * m * m * sizeof(double), s));
+  a.V = Vc;
+  CK(ks_launch_init(a, nt, cur, s));
+  ctx->launches++;
+  int k = 0;
+  bool first = true;
+  int restarts = 0;
+  float maxres = 0.f;
+  bool noconv = false;
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  for (;;) {
+    a.V = Vc;
+    long long active_px = 0;
+    for (int i = 0; i < np; i++)
+      if (active[i]) active_px += L.patches[i].N;
+    for (int j = k; j < m; j++) {
+      const bool from_v = (j == k && !first);
+      // algorithmic bytes per pixel: SpMV reads 40 upper coefficients, the
+      // diagonal and x, writes v_j and w, and reads j basis vectors for the
+      // dots; a CGS pass reads w and j+1 basis vectors and writes w
+      const double npx = (double)active_px;
+      prof_begin(ctx, 0, npx * 4.0 * (kUpper + 1 + 1 + 2 + j));
+      CK(ks_launch_spmv(a, nt, j, from_v ? Vc + (long long)k * L.lvec : cur, from_v ? 0 : 1, nxt, s));
+      prof_end(ctx);
+      prof_begin(ctx, 1, npx * 4.0 * (j + 1 + 2));
+      CK(ks_launch_orth(a, nt, j, 1, nxt, s));
+      prof_end(ctx);
+      prof_begin(ctx, 1, npx * 4.0 * (j + 1 + 2));
+      CK(ks_launch_orth(a, nt, j, 2, nxt, s));
+      prof_end(ctx);
+      ctx->launches += 3;
+      std::swap(cur, nxt);
+    }
+    CK(cudaMemcpyAsync(T.data(), b.T, T.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(beta2.data(), b.beta2, np * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    // host: dense eigensolve per active patch (threads over patches)
+    int active_count = 0;
+    for (int i = 0; i < np; i++) active_count += active[i];
+    std::atomic<int> next(0);
+    std::vector<float> res((size_t)np, 0.f);
+    auto worker = [&]() {
+      std::vector<double> A((size_t)m * m), w(m), Z((size_t)m * m);
+      for (int i; (i = next.fetch_add(1)) < np;) {
+        if (!active[i]) continue;
+        mv[i] += m - k;
+        const double* Ti = T.data() + (size_t)i * m * m;
+        for (int r = 0; r < m; r++)
+          for (int c = 0; c < m; c++) A[r * m + c] = 0.5 * (Ti[r * m + c] + Ti[c * m + r]);
+        gpb::sym_eig(A.data(), m, w.data(), Z.data());
+        const double beta = sqrt(beta2[i]);
+        double worst = 0;
+        for (int c = 0; c < nev; c++) worst = std::max(worst, fabs(beta * Z[(m - 1) * m + c]));
+        res[i] = (float)worst;
+        const bool conv = worst <= q.eig_tol;
+        const bool cap = mv[i] + (m - keep) > q.eig_max_matvecs;
+        double* Yi = Y.data() + (size_t)i * m * m;
+        for (int r = 0; r < m; r++)
+          for (int c = 0; c < m; c++) Yi[r * m + c] = Z[r * m + c];
+        if (conv || cap) {
+          decision[i] = 2;
+          nkeep[i] = nev;
+          for (int c = 0; c < nev; c++) evals[(size_t)i * nev + c] = (float)w[c];
+          if (!conv) noconv = true;
+        } else {
+          decision[i] = 1;
+          nkeep[i] = keep;
+          double* Tn = T.data() + (size_t)i * m * m;
+          std::fill(Tn, Tn + (size_t)m * m, 0.0);
+          for (int c = 0; c < keep; c++) {
+            Tn[c * m + c] = w[c];
+            Tn[c * m + keep] = Tn[keep * m + c] = beta * Z[(m - 1) * m + c];
+          }
+        }
+      }
+    };
+    {
+      // one dense solve takes ~0.1 ms: threads only pay off for many patches
+      const unsigned nth = std::min<unsigned>(hw, (unsigned)((active_count + 3) / 4));
+      std::vector<std::thread> th;
+      for (unsigned t = 1; t < nth; t++) th.emplace_back(worker);
+      worker();
+      for (auto& t : th) t.join();
+    }
+    restarts++;
+    bool any_restart = false;
+    for (int i = 0; i < np; i++) {
+      if (decision[i] == 2 && active[i]) {
+        active[i] = 0;
+        maxres = std::max(maxres, res[i]);
+      }
+      if (decision[i] == 1) any_restart = true;
+    }
+    CK(cudaMemcpyAsync(b.Y, Y.data(), Y.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.T, T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.decision, decision.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.nkeep, nkeep.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    a.V = Vc;
+    CK(ks_launch_restart(a, nt, std::max(keep, nev), cur, Va, b.evec, s));
+    ctx->launches++;
+    std::swap(Vc, Va);
+    std::fill(decision.begin(), decision.end(), 0);
+    CK(cudaMemcpyAsync(b.decision, decision.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (!any_restart) break;
+    k = keep;
+    first = false;
+  }
+  CK(cudaMemcpyAsync(b.evals, evals.data(), evals.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  prof_collect(ctx);
+  ctx->evals_host = evals;
+  long tot = 0, mx = 0;
+  for (int i = 0; i < np; i++) {
+    tot += mv[i];
+    mx = std::max(mx, (long)mv[i]);
+  }
+  ctx->stats.matvecs_total = tot;
+  ctx->stats.matvecs_max = mx;
+  ctx->stats.restarts = restarts;
+  ctx->stats.max_residual = maxres;
+  return noconv ? GPB_ERR_NOCONV : GPB_OK;
+}
+
+static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const uint32_t* hs,
+                            const uint32_t* const* host_in, const size_t* host_stride, const uint32_t* dev_in,
+                            const size_t* dev_off, float* dev_nmax, float* dev_orient, gpb_result* host_out) {
+  if (n == 0) return GPB_ERR_ARG;
+  if (ctx->K == 0) return GPB_ERR_ARG;  // no codebook
+  for (size_t i = 0; i < n; i++)
+    if (ws[i] < (uint32_t)kMinSide || hs[i] < (uint32_t)kMinSide || ws[i] > 8192 || hs[i] > 8192)
+      return GPB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->st;
+  Buf& b = ctx->b;
+  ctx->launches = 0;
+  memset(&ctx->stats, 0, sizeof(ctx->stats));
+  Layout L = make_layout(n, ws, hs);
+  std::string key;
+  for (size_t i = 0; i < n; i++) key += std::to_string(ws[i]) + "x" + std::to_string(hs[i]) + ",";
+  const bool changed = key != ctx->layout_key;
+  gpb_status st = ensure_buffers(ctx, L, changed);
+  if (st != GPB_OK) return st;
+  ctx->layout_key = key;
+  const size_t np = L.patches.size();
+  CK(cudaEventRecord(ctx->ev[0], s));
+  CK(cudaMemcpyAsync(b.patches, L.patches.data(), np * sizeof(PatchDev), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.work_tex, L.work_tex.data(), L.work_tex.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.work_cue, L.work_cue.data(), L.work_cue.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.work16, L.work16.data(), L.work16.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.tiles, L.tiles.data(), L.tiles.size() * sizeof(EigTile), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.tile_begin, L.tile_begin.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.tile_count, L.tile_count.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  // input
+  const uint32_t* d_packed = b.packed;
+  if (host_in) {
+    if (ctx->c_hpacked < (size_t)L.total_pix) {
+      if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
+      CK(cudaMallocHost(&ctx->h_packed, L.total_pix * sizeof(uint32_t)));
+      ctx->c_hpacked = L.total_pix;
+    }
+    for (size_t i = 0; i < n; i++) {
+      const PatchDev& P = L.patches[i];
+      for (int y = 0; y < P.H; y++)
+        memcpy(ctx->h_packed + P.pix + (size_t)y * P.W, host_in[i] + (size_t)y * host_stride[i],
+               (size_t)P.W * sizeof(uint32_t));
+    }
+    CK(cudaMemcpyAsync(b.packed, ctx->h_packed, L.total_pix * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  } else {
+    for (size_t i = 0; i < n; i++) {
+      const PatchDev& P = L.patches[i];
+      CK(cudaMemcpyAsync(b.packed + P.pix, dev_in + dev_off[i], (size_t)P.N * sizeof(uint32_t),
+                         cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  CK(cudaEventRecord(ctx->ev[1], s));
+  // (a) textons
+  CK(launch_convert(b.packed, L.total_pix, b.grey, b.lab4, s));
+  CK(cudaMemsetAsync(b.repair_count, 0, sizeof(int), s));
+  const int repair_cap = (int)(b.c_repair / 2);
+  CK(launch_texton(b.patches, b.work_tex, (int)L.work_tex.size(), b.grey, b.lab4, b.repair, b.repair_count,
+                   repair_cap, s));
+  CK(launch_texton_repair(b.patches, b.grey, b.lab4, b.repair, b.repair_count, repair_cap, ctx->d_k32_ring,
+                          ctx->d_ring_of, ctx->tab.n_rings, s));
+  CK(cudaEventRecord(ctx->ev[2], s));
+  // (b) local cues + NMS
+  CK(launch_maxlabel(b.patches, (int)np, b.lab4, b.nbins, s));
+  CK(launch_cues(b.patches, b.work_cue, (int)L.work_cue.size(), b.lab4, b.nbins, b.mpbo, b.go,
+                 ctx->prm.keep_intermediates ? b.raw : nullptr,
+                 ctx->prm.keep_intermediates >= 2 ? b.counts : nullptr, s));
+  CK(cudaEventRecord(ctx->ev[3], s));
+  CK(launch_nms(b.patches, b.work16, (int)L.work16.size(), b.mpbo, b.mpb, s));
+  CK(cudaEventRecord(ctx->ev[4], s));
+  // (c) buildW
+  CK(launch_buildw(b.patches, b.work16, (int)L.work16.size(), b.mpb, ctx->d_ic, b.wup, b.deg, L.lvec, s));
+  CK(launch_scale(b.patches, b.work16, (int)L.work16.size(), b.wup, b.deg, b.aup, b.adiag, b.dis, L.lvec,
+                  ctx->prm.keep_intermediates ? b.wfull : nullptr, s));
+  CK(cudaEventRecord(ctx->ev[5], s));
+  ctx->launches += 10;
+  // (d) eigensolver
+  gpb_status es = solve_lanczos(ctx, L);
+  if (es != GPB_OK && es != GPB_ERR_NOCONV) return es;
+  CK(cudaEventRecord(ctx->ev[6], s));
+  // (e) sPb + gPb
+  float* o_nmax = dev_nmax ? dev_nmax : b.nmax;
+  float* o_orient = dev_orient ? dev_orient : b.orient;
+  CK(launch_minmax(b.patches, (int)np, b.evec, L.lvec, b.dis, ctx->prm.nvec, b.mm, s));
+  CK(launch_spb(b.patches, b.work16, (int)L.work16.size(), b.evec, L.lvec, b.dis, b.evals, b.mm, ctx->prm.nvec,
+                b.go, b.mpb, ctx->prm.compat, ctx->prm.keep_intermediates ? b.spb : nullptr,
+                ctx->prm.keep_intermediates ? b.gpbo : nullptr, o_nmax, o_orient, s));
+  ctx->launches += 2;
+  CK(cudaEventRecord(ctx->ev[7], s));
+  if (host_out) {
+    const size_t need = 9 * (size_t)L.total_pix;
+    if (ctx->c_hout < need) {
+      if (ctx->h_out) cudaFreeHost(ctx->h_out);
+      CK(cudaMallocHost(&ctx->h_out, need * sizeof(float)));
+      ctx->c_hout = need;
+    }
+    CK(cudaMemcpyAsync(ctx->h_out, o_nmax, L.total_pix * sizeof(float), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ctx->h_out + L.total_pix, o_orient, 8 * L.total_pix * sizeof(float),
+                       cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaEventRecord(ctx->ev[8], s));
+  CK(cudaStreamSynchronize(s));
+  if (host_out) {
+    for (size_t i = 0; i < n; i++) {
+      const PatchDev& P = L.patches[i];
+      gpb_result& r = host_out[i];
+      if (!r.nmax) r.nmax = (float*)malloc((size_t)P.N * sizeof(float));
+      if (!r.orient) r.orient = (float*)malloc(8 * (size_t)P.N * sizeof(float));
+      if (!r.nmax || !r.orient) return GPB_ERR_NOMEM;
+      memcpy(r.nmax, ctx->h_out + P.pix, (size_t)P.N * sizeof(float));
+      memcpy(r.orient, ctx->h_out + L.total_pix + 8 * P.pix, 8 * (size_t)P.N * sizeof(float));
+    }
+  }
+  float ms[9];
+  for (int i = 1; i <= 8; i++) cudaEventElapsedTime(&ms[i], ctx->ev[i - 1], ctx->ev[i]);
+  ctx->stats.ms_h2d = ms[1];
+  ctx->stats.ms_texton = ms[2];
+  ctx->stats.ms_cues = ms[3];
+  ctx->stats.ms_nms = ms[4];
+  ctx->stats.ms_buildw = ms[5];
+  ctx->stats.ms_eig = ms[6];
+  ctx->stats.ms_spb = ms[7];
+  ctx->stats.ms_d2h = ms[8];
+  cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->ev[8]);
+  ctx->stats.ms_total = ms[0];
+  ctx->stats.gpu_launches = ctx->launches;
+  int rc = 0;
+  cudaMemcpy(&rc, b.repair_count, sizeof(int), cudaMemcpyDeviceToHost);
+  ctx->stats.texton_repaired = rc;
+  ctx->patches = L.patches;
+  ctx->total_pix = L.total_pix;
+  ctx->lvec = L.lvec;
+  if (cudaGetLastError() != cudaSuccess) return GPB_ERR_CUDA;
+  return es;
+}
+
+extern "C" gpb_status gpb_compute_batch(gpb_ctx* ctx, const gpb_patch* patches, size_t n, gpb_result* out) {
+  if (!ctx || !patches || !out || n == 0) return GPB_ERR_ARG;
+  std::vector<uint32_t> ws(n), hs(n);
+  std::vector<const uint32_t*> in(n);
+  std::vector<size_t> stride(n);
+  for (size_t i = 0; i < n; i++) {
+    if (!patches[i].packed_bgr) return GPB_ERR_ARG;
+    ws[i] = patches[i].width;
+    hs[i] = patches[i].height;
+    in[i] = patches[i].packed_bgr;
+    stride[i] = patches[i].stride ? patches[i].stride : patches[i].width;
+  }
+  return run_batch(ctx, n, ws.data(), hs.data(), in.data(), stride.data(), nullptr, nullptr, nullptr, nullptr,
+                   out);
+}
+
+extern "C" gpb_status gpb_compute(gpb_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* packed,
+                                  float** out_nmax, float** out_orient) {
+  if (!ctx || !packed || !out_nmax || !out_orient) return GPB_ERR_ARG;
+  gpb_patch p = {width, height, packed, width};
+  gpb_result r = {nullptr, nullptr};
+  gpb_status s = gpb_compute_batch(ctx, &p, 1, &r);
+  if (s != GPB_OK && s != GPB_ERR_NOCONV) {
+    free(r.nmax);
+    free(r.orient);
+    return s;
+  }
+  *out_nmax = r.nmax;
+  *out_orient = r.orient;
+  return s;
+}
+
+extern "C" gpb_status gpb_compute_batch_device(gpb_ctx* ctx, size_t n, const uint32_t* widths,
+                                               const uint32_t* heights, const size_t* offsets,
+                                               const uint32_t* d_packed, float* d_nmax, float* d_orient) {
+  if (!ctx || !widths || !heights || !offsets || !d_packed || !d_nmax || !d_orient || n == 0) return GPB_ERR_ARG;
+  // outputs are written in the library's compact layout, then moved to the
+  // caller's offsets when they differ
+  gpb_status s = run_batch(ctx, n, widths, heights, nullptr, nullptr, d_packed, offsets, nullptr, nullptr, nullptr);
+  if (s != GPB_OK && s != GPB_ERR_NOCONV) return s;
+  for (size_t i = 0; i < n; i++) {
+    const PatchDev& P = ctx->patches[i];
+    CK(cudaMemcpyAsync(d_nmax + offsets[i], ctx->b.nmax + P.pix, (size_t)P.N * sizeof(float),
+                       cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_orient + 8 * offsets[i], ctx->b.orient + 8 * P.pix, 8 * (size_t)P.N * sizeof(float),
+                       cudaMemcpyDeviceToDevice, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  return s;
+}
+
+extern "C" gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st) {
+  if (!ctx || !st) return GPB_ERR_ARG;
+  *st = ctx->stats;
+  return GPB_OK;
+}
+
+extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst, size_t bytes) {
+  if (!ctx || !dst || patch >= ctx->patches.size()) return GPB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  const PatchDev& P = ctx->patches[patch];
+  const size_t N = P.N;
+  Buf& b = ctx->b;
+  const int nvec = ctx->prm.nvec;
+  auto need = [&](size_t x) { return bytes >= x; };
+  cudaError_t e = cudaSuccess;
+  switch (stage) {
+    case GPB_STAGE_TEXTON:
+    case GPB_STAGE_LABBINS: {
+      std::vector<uint32_t> v(N);
+      e = cudaMemcpy(v.data(), b.lab4 + P.pix, N * 4, cudaMemcpyDeviceToHost);
+      uint8_t* o = (uint8_t*)dst;
+      if (stage == GPB_STAGE_TEXTON) {
+        if (!need(N)) return GPB_ERR_ARG;
+        for (size_t i = 0; i < N; i++) o[i] = (uint8_t)(v[i] >> 24);
+      } else {
+        if (!need(3 * N)) return GPB_ERR_ARG;
+        for (int c = 0; c < 3; c++)
+          for (size_t i = 0; i < N; i++) o[c * N + i] = (uint8_t)((v[i] >> (8 * c)) & 255);
+      }
+      break;
+    }
+    case GPB_STAGE_MPB_O:
+      if (!need(8 * N * 4)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.mpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_MPB:
+      if (!need(N * 4)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.mpb + P.pix, N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_W:
+      if (!b.wfull || !need(81 * N * 4)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.wfull + 81 * P.pix, 81 * N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_EVALS:
+      if (!need((size_t)nvec * 4) || ctx->evals_host.size() < (patch + 1) * nvec) return GPB_ERR_ARG;
+      memcpy(dst, ctx->evals_host.data() + patch * nvec, (size_t)nvec * 4);
+      break;
+    case GPB_STAGE_EVECS:
+      if (!need((size_t)nvec * N * 4)) return GPB_ERR_ARG;
+      for (int i = 0; i < nvec && e == cudaSuccess; i++)
+        e = cudaMemcpy((float*)dst + i * N, b.evec + (size_t)i * ctx->lvec + P.vec, N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_SPB:
+      if (!b.spb || !need(8 * N * 4)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.spb + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_CUES:
+      if (!b.raw || !need(96 * N * 4)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.raw + 96 * P.pix, 96 * N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_GPB_O:
+      if (!b.gpbo || !need(8 * N * 4)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.gpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
+      break;
+    case GPB_STAGE_COUNTS: {
+      const size_t per = (size_t)kNannulus * 4 * 32 * 32;
+      if (!b.counts || !need(per * N)) return GPB_ERR_ARG;
+      e = cudaMemcpy(dst, b.counts + per * P.pix, per * N, cudaMemcpyDeviceToHost);
+      break;
+    }
+    default:
+      return GPB_ERR_ARG;
+  }
+  return e == cudaSuccess ? GPB_OK : GPB_ERR_CUDA;
+}

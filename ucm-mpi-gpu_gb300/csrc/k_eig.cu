@@ -1,0 +1,356 @@
+// k_eig.cu -- batched Krylov-Schur (thick-restart Lanczos) kernels for the
+// smallest eigenpairs of A = I - D^-1/2 W D^-1/2 (sm_103a).
+//
+// Reference: the Lanczos eigensolver of
+// damascene/src/noReorthog/lanczos.cu:192-752 and the stencil SpMV of
+// damascene/src/stencilMatrixMultiply/stencilMVM.cu:129-182; the CPU path's
+// Spectra SymGEigsSolver (src/spectralPb.cpp:221-245) defines the problem.
+//
+// One Lanczos step for every active patch of the batch is three launches:
+//   ks_spmv   w = A v_j (FP32 symmetric stencil SpMV, the lower triangle read
+//             as the upper array shifted by the offset), v_j = w_prev / beta
+//             written on the fly, h = V^T w
+//   ks_orth   w -= V h, h2 = V^T w          (classical Gram-Schmidt, pass 1)
+//   ks_orth   w -= V h2, beta^2 = |w|^2     (pass 2)
+// Dot products are accumulated in compensated FP32 (float-float: exact
+// product error by FMA plus two-sum), about as accurate as FP64
+// accumulation, whose rate on this part is 1/64 of FP32; the per-CTA
+// partials are reduced in FP64 by the last CTA of each patch to finish
+// (threadfence + atomic counter), so no separate reduction launches.
+// The projected matrix T lives in device memory; at the end of a restart
+// cycle the host solves it (eig_host.cpp) and ks_restart assembles the kept
+// Ritz vectors in place with compensated sums.
+#include <stdint.h>
+
+#include "gpb_internal.h"
+#include "kernels.h"
+#include "k_eig.h"
+
+namespace gpb {
+
+__constant__ int c_up_dy[kUpper], c_up_dx[kUpper];
+
+void upload_eig(const HostTables& t, cudaStream_t s) {
+  int dy[kUpper], dx[kUpper];
+  for (int j = 0; j < kUpper; j++) {
+    dy[j] = t.sdy[kStencilN / 2 + 1 + j];
+    dx[j] = t.sdx[kStencilN / 2 + 1 + j];
+  }
+  cudaMemcpyToSymbolAsync(c_up_dy, dy, sizeof(dy), 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_up_dx, dx, sizeof(dx), 0, cudaMemcpyHostToDevice, s);
+}
+
+constexpr unsigned FULLM = 0xffffffffu;
+
+__device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float a, float b) {
+  const float p = a * b;
+  const float pe = fmaf(a, b, -p);
+  const float s = hi + p;
+  const float z = s - hi;
+  const float e = (hi - (s - z)) + (p - z);
+  hi = s;
+  lo += e + pe;
+}
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float bhi, float blo) {
+  const float s = hi + bhi;
+  const float z = s - hi;
+  const float e = (hi - (s - z)) + (bhi - z);
+  hi = s;
+  lo += e + blo;
+}
+__device__ __forceinline__ double ff_warp_reduce(float hi, float lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(FULLM, hi, o), l2 = __shfl_xor_sync(FULLM, lo, o);
+    ff_add(hi, lo, h2, l2);
+  }
+  return (double)hi + (double)lo;
+}
+
+// Last CTA of a patch: returns true in every thread of that CTA.
+__device__ __forceinline__ bool last_cta(int* counter, int ntiles) {
+  __shared__ int is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int prev = atomicAdd(counter, 1);
+    is_last = (prev == ntiles - 1);
+    if (is_last) *counter = 0;
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// per-warp partial sums (sred[warp][i], written by lane 0) -> one partial per
+// CTA in part[cta][i]
+constexpr int kRed = kMaxKrylov + 1;
+__device__ __forceinline__ void cta_partials(const double* sred, int nvals, double* part_row) {
+  __syncthreads();
+  for (int i = threadIdx.x; i < nvals; i += blockDim.x) {
+    double s = 0;
+#pragma unroll
+    for (int w = 0; w < kEigWarps; w++) s += sred[w * kRed + i];
+    part_row[i] = s;
+  }
+}
+// sum of one value over the CTAs of a patch, one warp, lanes strided
+__device__ __forceinline__ double patch_sum(const double* part, int tb, int tc, int mp1, int i, int lane) {
+  double s = 0;
+  for (int b = tb + lane; b < tb + tc; b += 32) s += part[(long long)b * mp1 + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULLM, s, o);
+  return s;
+}
+
+// ------------------------------------------------------------------ SpMV
+__global__ void __launch_bounds__(kEigThreads) ks_spmv(EigArgs a, int j, const float* __restrict__ src,
+                                                       int use_beta, float* __restrict__ dst) {
+  const EigTile t = a.tiles[blockIdx.x];
+  if (!a.active[t.patch]) return;
+  const PatchDev P = a.patches[t.patch];
+  __shared__ long long off[kUpper];
+  if (threadIdx.x < kUpper) off[threadIdx.x] = (long long)c_up_dy[threadIdx.x] * P.W + c_up_dx[threadIdx.x];
+  __syncthreads();
+  const float inv = use_beta ? (float)(1.0 / sqrt(a.beta2[t.patch])) : 1.f;
+  const long long base = P.vec;
+  float wv[kEigPix], xv[kEigPix];
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    wv[r] = 0.f;
+    xv[r] = 0.f;
+    if (p >= t.p1) continue;
+    const long long q = base + p;
+    const float x = src[q] * inv;
+    float acc = 0.f;
+#pragma unroll 8
+    for (int k = 0; k < kUpper; k++) {
+      const float* au = a.a_up + (long long)k * a.lvec;
+      acc = fmaf(au[q], src[q + off[k]], acc);
+      acc = fmaf(au[q - off[k]], src[q - off[k]], acc);
+    }
+    xv[r] = x;
+    wv[r] = fmaf(acc, inv, a.a_diag[q] * x);
+  }
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    if (p >= t.p1) continue;
+    const long long q = base + p;
+    a.V[(long long)j * a.lvec + q] = xv[r];
+    dst[q] = wv[r];
+  }
+  // h_i = v_i . w for i <= j
+  __shared__ double sred[kEigWarps * kRed];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = 0; i <= j; i++) {
+    float hi = 0.f, lo = 0.f;
+#pragma unroll
+    for (int r = 0; r < kEigPix; r++) {
+      const int p = t.p0 + threadIdx.x + r * kEigThreads;
+      if (p >= t.p1) continue;
+      const float v = (i == j) ? xv[r] : a.V[(long long)i * a.lvec + base + p];
+      ff_add_prod(hi, lo, v, wv[r]);
+    }
+    const double s = ff_warp_reduce(hi, lo);
+    if (lane == 0) sred[warp * kRed + i] = s;
+  }
+  cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
+  if (last_cta(a.counter + t.patch, a.tile_count[t.patch])) {
+    const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
+    double* T = a.T + (long long)t.patch * a.m * a.m;
+    for (int i = warp; i <= j; i += kEigWarps) {
+      const double s = patch_sum(a.part, tb, tc, a.mp1, i, lane);
+      if (lane == 0) {
+        a.hbuf[(long long)t.patch * a.mp1 + i] = s;
+        T[i * a.m + j] = s;
+        T[j * a.m + i] = s;
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------- CGS pass
+// mode 1: w -= V h, then h2 = V^T w;  mode 2: w -= V h2, then |w|^2
+__global__ void __launch_bounds__(kEigThreads) ks_orth(EigArgs a, int j, int mode, float* __restrict__ w) {
+  const EigTile t = a.tiles[blockIdx.x];
+  if (!a.active[t.patch]) return;
+  const PatchDev P = a.patches[t.patch];
+  const long long base = P.vec;
+  __shared__ float hs[kMaxKrylov + 1];
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (float)a.hbuf[(long long)t.patch * a.mp1 + i];
+  __syncthreads();
+  float wv[kEigPix];
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    wv[r] = p < t.p1 ? w[base + p] : 0.f;
+  }
+  for (int i = 0; i <= j; i++) {
+    const float h = hs[i];
+#pragma unroll
+    for (int r = 0; r < kEigPix; r++) {
+      const int p = t.p0 + threadIdx.x + r * kEigThreads;
+      if (p < t.p1) wv[r] = fmaf(-h, a.V[(long long)i * a.lvec + base + p], wv[r]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    if (p < t.p1) w[base + p] = wv[r];
+  }
+  __shared__ double sred[kEigWarps * kRed];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (mode == 1) {
+    for (int i = 0; i <= j; i++) {
+      float hi = 0.f, lo = 0.f;
+#pragma unroll
+      for (int r = 0; r < kEigPix; r++) {
+        const int p = t.p0 + threadIdx.x + r * kEigThreads;
+        if (p < t.p1) ff_add_prod(hi, lo, a.V[(long long)i * a.lvec + base + p], wv[r]);
+      }
+      const double s = ff_warp_reduce(hi, lo);
+      if (lane == 0) sred[warp * kRed + i] = s;
+    }
+    cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
+  } else {
+    float hi = 0.f, lo = 0.f;
+#pragma unroll
+    for (int r = 0; r < kEigPix; r++) ff_add_prod(hi, lo, wv[r], wv[r]);
+    const double s = ff_warp_reduce(hi, lo);
+    if (lane == 0) sred[warp * kRed] = s;
+    cta_partials(sred, 1, a.part + (long long)blockIdx.x * a.mp1);
+  }
+  if (last_cta(a.counter + t.patch, a.tile_count[t.patch])) {
+    const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
+    double* T = a.T + (long long)t.patch * a.m * a.m;
+    if (mode == 1) {
+      for (int i = warp; i <= j; i += kEigWarps) {
+        const double s = patch_sum(a.part, tb, tc, a.mp1, i, lane);
+        if (lane == 0) {
+          a.hbuf[(long long)t.patch * a.mp1 + i] = s;
+          T[i * a.m + j] += s;
+          if (i != j) T[j * a.m + i] += s;
+        }
+      }
+    } else if (warp == 0) {
+      double s = patch_sum(a.part, tb, tc, a.mp1, 0, lane);
+      if (lane != 0) return;
+      if (!(s > 1e-60)) s = 1e-60;
+      a.beta2[t.patch] = s;
+      if (j + 1 < a.m) {
+        const double b = sqrt(s);
+        T[(j + 1) * a.m + j] = b;
+        T[j * a.m + (j + 1)] = b;
+      }
+    }
+  }
+}
+
+// -------------------------------------------------------------- restart
+// Vout[:, 0..nk) = V[:, 0..m) Y[:, 0..nk) per pixel, 8 outputs at a time with
+// compensated sums (Y split into FP32 hi + lo), then Vout[nk] = w / beta
+// (restart, Vout is the other basis buffer) -- or, for a converged patch,
+// the nk = nvec Ritz vectors into evec_out.
+__global__ void __launch_bounds__(kEigThreads) ks_restart(EigArgs a, const float* __restrict__ w,
+                                                          float* __restrict__ vout,
+                                                          float* __restrict__ evec_out) {
+  const EigTile t = a.tiles[blockIdx.x];
+  const int mode = a.decision[t.patch];  // 0 idle, 1 restart, 2 final
+  if (mode == 0) return;
+  const PatchDev P = a.patches[t.patch];
+  const int nk = a.nkeep[t.patch];
+  extern __shared__ float ysh[];  // [m][nk] hi, then lo
+  const double* Y = a.Y + (long long)t.patch * a.m * a.m;
+  for (int idx = threadIdx.x; idx < a.m * nk; idx += blockDim.x) {
+    const int i = idx / nk, c = idx % nk;
+    const double y = Y[i * a.m + c];
+    const float hi = (float)y;
+    ysh[idx] = hi;
+    ysh[a.m * nk + idx] = (float)(y - (double)hi);
+  }
+  __syncthreads();
+  const float inv = (float)(1.0 / sqrt(a.beta2[t.patch]));
+  const long long base = P.vec;
+  float* out = (mode == 1) ? vout : evec_out;
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    if (p >= t.p1) continue;
+    for (int c0 = 0; c0 < nk; c0 += 8) {
+      float hi[8], lo[8];
+#pragma unroll
+      for (int c = 0; c < 8; c++) hi[c] = lo[c] = 0.f;
+      for (int i = 0; i < a.m; i++) {
+        const float v = a.V[(long long)i * a.lvec + base + p];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          if (c0 + c < nk) {
+            ff_add_prod(hi[c], lo[c], ysh[i * nk + c0 + c], v);
+            lo[c] = fmaf(ysh[a.m * nk + i * nk + c0 + c], v, lo[c]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        if (c0 + c < nk) out[(long long)(c0 + c) * a.lvec + base + p] = hi[c] + lo[c];
+    }
+    if (mode == 1) vout[(long long)nk * a.lvec + base + p] = w[base + p] * inv;
+  }
+}
+
+// start vector: a fixed hash per pixel, |w|^2 into beta2 (through the same
+// last-CTA reduction)
+__device__ __forceinline__ float hash_unit(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return (float)(x & 0xffffff) * (1.0f / 16777216.0f) - 0.5f;
+}
+
+__global__ void __launch_bounds__(kEigThreads) ks_init(EigArgs a, float* __restrict__ w) {
+  const EigTile t = a.tiles[blockIdx.x];
+  if (!a.active[t.patch]) return;
+  const PatchDev P = a.patches[t.patch];
+  float hi = 0.f, lo = 0.f;
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    if (p >= t.p1) continue;
+    const float v = hash_unit((uint32_t)p * 2654435761u + 12345u);
+    w[P.vec + p] = v;
+    ff_add_prod(hi, lo, v, v);
+  }
+  __shared__ double sred[kEigWarps * kRed];
+  const double s = ff_warp_reduce(hi, lo);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sred[warp * kRed] = s;
+  cta_partials(sred, 1, a.part + (long long)blockIdx.x * a.mp1);
+  if (last_cta(a.counter + t.patch, a.tile_count[t.patch]) && warp == 0) {
+    const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
+    const double s2 = patch_sum(a.part, tb, tc, a.mp1, 0, lane);
+    if (lane == 0) a.beta2[t.patch] = s2;
+  }
+}
+
+cudaError_t ks_launch_init(const EigArgs& a, int ntiles, float* w, cudaStream_t s) {
+  ks_init<<<ntiles, kEigThreads, 0, s>>>(a, w);
+  return cudaGetLastError();
+}
+cudaError_t ks_launch_spmv(const EigArgs& a, int ntiles, int j, const float* src, int use_beta,
+                           float* dst, cudaStream_t s) {
+  ks_spmv<<<ntiles, kEigThreads, 0, s>>>(a, j, src, use_beta, dst);
+  return cudaGetLastError();
+}
+cudaError_t ks_launch_orth(const EigArgs& a, int ntiles, int j, int mode, float* w, cudaStream_t s) {
+  ks_orth<<<ntiles, kEigThreads, 0, s>>>(a, j, mode, w);
+  return cudaGetLastError();
+}
+cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, int max_nk, const float* w, float* vout,
+                              float* evec, cudaStream_t s) {
+  ks_restart<<<ntiles, kEigThreads, 2 * a.m * max_nk * sizeof(float), s>>>(a, w, vout, evec);
+  return cudaGetLastError();
+}
+
+}  // namespace gpb

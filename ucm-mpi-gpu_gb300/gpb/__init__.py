@@ -1,0 +1,216 @@
+"""Host-side mirror of the reference's gPb boundary over libgpb's C ABI.
+
+``GlobalPbCuda`` mirrors ``GlobalPbCuda`` of src/globalPb.cpp:247-313 (a BGR
+uint8 patch in, 8 orientation planes and the nonmax plane out, as float64
+H x W arrays); ``compute_gpb`` mirrors ``computeGPb`` of
+damascene/include/globalPb.h:35 (packed uint32 in, flat float32 buffers
+out).  ``Context`` exposes the batched entry points.  Every call goes to the
+CUDA library; there is no CPU path, and a missing library raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import synth  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "libgpb.so")
+
+GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT = range(6)
+COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
+EIG_LANCZOS, EIG_WARM = 0, 1
+STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
+          "spb": 7, "cues": 8, "gpb_o": 9, "counts": 10}
+
+
+class GpbError(RuntimeError):
+    def __init__(self, status, what):
+        super().__init__("%s: %s (status %d)" % (what, _lib().gpb_status_str(status).decode(), status))
+        self.status = status
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("compat", ctypes.c_int), ("nvec", ctypes.c_int),
+                ("eig_tol", ctypes.c_float), ("eig_max_matvecs", ctypes.c_int),
+                ("krylov_dim", ctypes.c_int), ("krylov_keep", ctypes.c_int),
+                ("eig_mode", ctypes.c_int), ("keep_intermediates", ctypes.c_int)]
+
+
+class Patch(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("packed_bgr", ctypes.c_void_p), ("stride", ctypes.c_size_t)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("nmax", ctypes.c_void_p), ("orient", ctypes.c_void_p)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("ms_total", "ms_h2d", "ms_texton", "ms_cues", "ms_nms",
+                                              "ms_buildw", "ms_eig", "ms_spb", "ms_d2h")] + [
+        ("matvecs_max", ctypes.c_long), ("matvecs_total", ctypes.c_long), ("restarts", ctypes.c_int),
+        ("max_residual", ctypes.c_float), ("texton_repaired", ctypes.c_long),
+        ("gpu_launches", ctypes.c_int), ("spmv_ms", ctypes.c_double), ("orth_ms", ctypes.c_double),
+        ("spmv_launches", ctypes.c_long), ("orth_launches", ctypes.c_long),
+        ("spmv_bytes", ctypes.c_double), ("orth_bytes", ctypes.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+_L = None
+
+
+def _lib():
+    global _L
+    if _L is None:
+        if not os.path.exists(LIBPATH):
+            raise RuntimeError("libgpb.so is not built; run __graft_entry__.build() or "
+                               "python ucm-mpi-gpu_gb300/gpb/build.py")
+        L = ctypes.CDLL(LIBPATH)
+        vp, c, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+        L.gpb_default_params.argtypes = [ctypes.POINTER(Params)]
+        L.gpb_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Params)]
+        L.gpb_create.restype = c
+        L.gpb_destroy.argtypes = [vp]
+        L.gpb_set_codebook.argtypes = [vp, vp, c]
+        L.gpb_set_codebook.restype = c
+        L.gpb_load_codebook_yml.argtypes = [vp, ctypes.c_char_p]
+        L.gpb_load_codebook_yml.restype = c
+        L.gpb_compute.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.POINTER(vp),
+                                  ctypes.POINTER(vp)]
+        L.gpb_compute.restype = c
+        L.gpb_compute_batch.argtypes = [vp, ctypes.POINTER(Patch), sz, ctypes.POINTER(Result)]
+        L.gpb_compute_batch.restype = c
+        L.gpb_compute_batch_device.argtypes = [vp, sz, vp, vp, vp, vp, vp, vp]
+        L.gpb_compute_batch_device.restype = c
+        L.gpb_fetch.argtypes = [vp, c, sz, vp, sz]
+        L.gpb_fetch.restype = c
+        L.gpb_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.gpb_last_stats.restype = c
+        L.gpb_device_count.restype = c
+        L.gpb_status_str.argtypes = [c]
+        L.gpb_status_str.restype = ctypes.c_char_p
+        L.gpb_free.argtypes = [vp]
+        _L = L
+    return _L
+
+
+def default_params(**kw):
+    p = Params()
+    _lib().gpb_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def device_count():
+    return _lib().gpb_device_count()
+
+
+def _check(st, what, allow_noconv=False):
+    if st == GPB_OK or (allow_noconv and st == GPB_ERR_NOCONV):
+        return
+    raise GpbError(st, what)
+
+
+class Context:
+    """One libgpb context (device buffers, stream, tables)."""
+
+    def __init__(self, codebook=None, **params):
+        self._h = ctypes.c_void_p()
+        self.params = default_params(**params)
+        _check(_lib().gpb_create(ctypes.byref(self._h), ctypes.byref(self.params)), "gpb_create")
+        if codebook is not None:
+            self.set_codebook(codebook)
+
+    def close(self):
+        if self._h:
+            _lib().gpb_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_codebook(self, codebook):
+        cb = np.ascontiguousarray(codebook, np.float32)
+        if cb.ndim != 2 or cb.shape[0] != 13:
+            raise ValueError("codebook must be 13 x K")
+        _check(_lib().gpb_set_codebook(self._h, cb.ctypes.data, cb.shape[1]), "gpb_set_codebook")
+
+    def load_codebook_yml(self, path):
+        _check(_lib().gpb_load_codebook_yml(self._h, path.encode()), "gpb_load_codebook_yml")
+
+    def compute_batch(self, packed_list):
+        """packed_list: uint32 H x W arrays (B<<16|G<<8|R).  Returns a list of
+        (nmax H x W, orient 8*H*W flat) float32 arrays in the context's layout."""
+        n = len(packed_list)
+        arrs = [np.ascontiguousarray(a, np.uint32) for a in packed_list]
+        pt = (Patch * n)()
+        res = (Result * n)()
+        outs = []
+        for i, a in enumerate(arrs):
+            H, W = a.shape
+            nm = np.empty((H, W), np.float32)
+            orr = np.empty(8 * H * W, np.float32)
+            outs.append((nm, orr))
+            pt[i] = Patch(W, H, a.ctypes.data, W)
+            res[i] = Result(nm.ctypes.data, orr.ctypes.data)
+        st = _lib().gpb_compute_batch(self._h, pt, n, res)
+        _check(st, "gpb_compute_batch", allow_noconv=True)
+        self.last_status = st
+        return outs
+
+    def compute_batch_device(self, widths, heights, offsets, d_packed, d_nmax, d_orient):
+        """Device-resident batch; the d_* arguments are raw device pointers."""
+        n = len(widths)
+        w = np.ascontiguousarray(widths, np.uint32)
+        h = np.ascontiguousarray(heights, np.uint32)
+        o = np.ascontiguousarray(offsets, np.uint64)
+        st = _lib().gpb_compute_batch_device(self._h, n, w.ctypes.data, h.ctypes.data, o.ctypes.data,
+                                             d_packed, d_nmax, d_orient)
+        _check(st, "gpb_compute_batch_device", allow_noconv=True)
+        self.last_status = st
+        return st
+
+    def fetch(self, stage, patch, shape, dtype):
+        out = np.empty(shape, dtype)
+        _check(_lib().gpb_fetch(self._h, STAGES[stage], patch, out.ctypes.data, out.nbytes), "gpb_fetch")
+        return out
+
+    def stats(self):
+        s = Stats()
+        _check(_lib().gpb_last_stats(self._h, ctypes.byref(s)), "gpb_last_stats")
+        return s.as_dict()
+
+
+def compute_gpb(ctx, packed):
+    """computeGPb (damascene/include/globalPb.h:35) on one packed H x W patch:
+    returns (hostGPb H*W, hostGPbAllConcat 8*H*W) as flat float32 arrays in
+    the layout of the context's compat mode."""
+    nm, orr = ctx.compute_batch([packed])[0]
+    return nm.ravel(), orr
+
+
+def GlobalPbCuda(ctx, image_patch, out_file="", n_orient=8, rank=0, rsz=1.0):
+    """Mirror of GlobalPbCuda (src/globalPb.cpp:247-313): BGR uint8 H x W x 3
+    patch in; returns (gPbOrient: list of n_orient float64 H x W planes,
+    gPbNonmax: float64 H x W).  out_file and rsz are unused, as in the
+    reference; rank selects nothing here (one context, one device)."""
+    img = np.ascontiguousarray(image_patch, np.uint8)
+    if img.ndim != 3 or img.shape[2] != 3:
+        raise ValueError("expected an H x W x 3 BGR uint8 patch")
+    H, W, _ = img.shape
+    packed = synth.pack_bgr(img)
+    nm, orr = ctx.compute_batch([packed])[0]
+    if ctx.params.compat == COMPAT_DAMASCENE:
+        # hostGPbAllConcat[o*rows*cols + j*rows + i] (src/globalPb.cpp:297)
+        planes = orr.reshape(8, W, H).transpose(0, 2, 1)
+    else:
+        planes = orr.reshape(8, H, W)
+    orient = [planes[o].astype(np.float64) for o in range(n_orient)]
+    return orient, nm.reshape(H, W).astype(np.float64)
