@@ -65,6 +65,7 @@ typedef struct {
   int krylov_keep;       /* vectors kept at a restart                             */
   int eig_mode;          /* gpb_eig_mode                                          */
   int keep_intermediates;/* 1: retain per-stage buffers for gpb_fetch(); 2: also counts */
+  int cheb_degree;       /* Chebyshev filter degree of the block solver          */
 } gpb_params;
 
 typedef struct gpb_ctx gpb_ctx;

@@ -1086,10 +1086,13 @@ void orc_oefilter(double theta, double* out) {
 /* src/spectralPb.cpp:269-322: eigenvectors 1..nvec-1 (ascending, D11),
  * v = D^-1/2 y min-max normalised then divided by sqrt(lambda); 8 oriented
  * filters at theta = o*pi/8 applied with filter2D semantics (correlation,
- * BORDER_REFLECT_101) and |.| accumulated into slot ch_per[o]. */
+ * BORDER_REFLECT_101) and |.| accumulated into slot ch_per[o].  The
+ * reference's ch_per {3,2,1,0,7,6,5,4} (spectralPb.cpp:289) goes with its own
+ * defective filter; with the fixed filter (D3) the slot that makes sPb_o
+ * peak at the same orientation as the local cues is (4 - o) mod 8. */
 void orc_spb(const double* evals, const double* evecs, const double* dis, int H, int W, int nvec,
              double* spb) {
-  static const int ch_per[8] = {3, 2, 1, 0, 7, 6, 5, 4};
+  static const int ch_per[8] = {4, 3, 2, 1, 0, 7, 6, 5};
   const size_t N = (size_t)H * W;
   double filt[8][49];
   for (int o = 0; o < 8; o++) orc_oefilter((REF_PI / 8) * (double)o, filt[o]);

@@ -20,6 +20,7 @@
 
 #include "../../include/gpb.h"
 #include "gpb_internal.h"
+#include "k_block.h"
 #include "k_eig.h"
 #include "kernels.h"
 
@@ -95,9 +96,19 @@ struct Buf {
   int4* work_tex = nullptr; size_t c_wt = 0;
   int4* work_cue = nullptr; size_t c_wc = 0;
   int4* work16 = nullptr; size_t c_w16 = 0;
+  int4* work_blk = nullptr; size_t c_wb = 0;
   EigTile* tiles = nullptr; size_t c_tiles = 0;
   int* tile_begin = nullptr; size_t c_tb = 0;
   int* tile_count = nullptr; size_t c_tc = 0;
+  // block solver
+  float* blk[4] = {nullptr, nullptr, nullptr, nullptr}; size_t c_blk[4] = {0, 0, 0, 0};
+  double* bpart = nullptr; size_t c_bpart = 0;
+  double* bgram = nullptr; size_t c_bgram = 0;
+  double* bmat = nullptr; size_t c_bmat = 0;
+  double* btheta = nullptr; size_t c_btheta = 0;
+  double* bres = nullptr; size_t c_bres = 0;
+  float3* bcoef = nullptr; size_t c_bcoef = 0;
+  int* bdone = nullptr; size_t c_bdone = 0;
 };
 
 struct gpb_ctx {
@@ -124,6 +135,7 @@ struct gpb_ctx {
   cudaEvent_t ev[12];
   // optional per-kernel timing of the eigensolver launches
   bool profile = false;
+  bool trace = false;
   std::vector<cudaEvent_t> pev;
   std::vector<int> pkind;      // 0 spmv, 1 orth
   std::vector<double> pbytes;  // algorithmic bytes of that launch
@@ -173,12 +185,13 @@ extern "C" void gpb_default_params(gpb_params* p) {
   p->device = -1;
   p->compat = GPB_COMPAT_CPU;
   p->nvec = 9;
-  p->eig_tol = 3e-6f;
+  p->eig_tol = 1e-6f;
   p->eig_max_matvecs = 20000;
   p->krylov_dim = 40;
   p->krylov_keep = 26;
   p->eig_mode = GPB_EIG_LANCZOS;
   p->keep_intermediates = 0;
+  p->cheb_degree = 40;
 }
 
 extern "C" const char* gpb_status_str(gpb_status s) {
@@ -229,6 +242,8 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
   {
     const char* pe = getenv("GPB_PROFILE");
     ctx->profile = pe && pe[0] == '1';
+    const char* tr = getenv("GPB_TRACE");
+    ctx->trace = tr && tr[0] == '1';
   }
   build_tables(ctx->tab, q.compat);
   cudaStream_t s = ctx->st;
@@ -237,6 +252,7 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
   upload_buildw(ctx->tab, s);
   upload_eig(ctx->tab, s);
   upload_spb(ctx->tab, s);
+  upload_block(ctx->tab, s);
   // global tables: IC paths, FP64 ring coefficients and the offset->ring map
   size_t nic = ctx->tab.ic.size();
   std::vector<int> ring_of(2401);
@@ -279,8 +295,10 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
   void* ptrs[] = {b.packed, b.grey, b.lab4, b.nbins, b.repair, b.repair_count, b.mpbo, b.go, b.mpb, b.raw,
                   b.wfull, b.counts, b.wup, b.aup, b.deg, b.dis, b.adiag, b.V[0], b.V[1], b.W[0], b.W[1], b.evec,
                   b.part, b.hbuf, b.T, b.Y, b.beta2, b.counter, b.active, b.decision, b.nkeep, b.evals,
-                  b.mm, b.spb, b.gpbo, b.nmax, b.orient, b.patches, b.work_tex, b.work_cue, b.work16,
-                  b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of};
+                  b.mm, b.spb, b.gpbo, b.nmax, b.orient, b.patches, b.work_tex, b.work_cue, b.work16, b.work_blk,
+                  b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
+                  b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
+                  b.bcoef, b.bdone};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
@@ -344,7 +362,7 @@ namespace {
 
 struct Layout {
   std::vector<PatchDev> patches;
-  std::vector<int4> work_tex, work_cue, work16;
+  std::vector<int4> work_tex, work_cue, work16, work_blk;
   std::vector<EigTile> tiles;
   std::vector<int> tile_begin, tile_count;
   long long total_pix = 0, lvec = 0;
@@ -376,6 +394,8 @@ Layout make_layout(size_t n, const uint32_t* ws, const uint32_t* hs) {
       }
     for (int y = 0; y < P.H; y += kCueTileH)
       for (int x = 0; x < P.W; x += kCueTileW) L.work_cue.push_back(make_int4(pi, y, x, 0));
+    for (int y = 0; y < P.H; y += kStepTileH)
+      for (int x = 0; x < P.W; x += kStepTileW) L.work_blk.push_back(make_int4(pi, y, x, 0));
     L.tile_begin.push_back((int)L.tiles.size());
     for (int p0 = 0; p0 < P.N; p0 += kEigTile) {
       EigTile t;
@@ -444,9 +464,20 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
   es.push_back(grow(b.work_tex, b.c_wt, L.work_tex.size()));
   es.push_back(grow(b.work_cue, b.c_wc, L.work_cue.size()));
   es.push_back(grow(b.work16, b.c_w16, L.work16.size()));
+  es.push_back(grow(b.work_blk, b.c_wb, L.work_blk.size()));
   es.push_back(grow(b.tiles, b.c_tiles, nt));
   es.push_back(grow(b.tile_begin, b.c_tb, np));
   es.push_back(grow(b.tile_count, b.c_tc, np));
+  if (q.eig_mode == GPB_EIG_WARM) {
+    for (int i = 0; i < 4; i++) es.push_back(grow(b.blk[i], b.c_blk[i], (size_t)kBlk * V));
+    es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
+    es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
+    es.push_back(grow(b.bmat, b.c_bmat, np * kBlk * kBlk));
+    es.push_back(grow(b.btheta, b.c_btheta, np * kBlk));
+    es.push_back(grow(b.bres, b.c_bres, np * kBlk));
+    es.push_back(grow(b.bcoef, b.c_bcoef, np * (size_t)kMaxCheb));
+    es.push_back(grow(b.bdone, b.c_bdone, np));
+  }
   for (cudaError_t e : es)
     if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? GPB_ERR_NOMEM : GPB_ERR_CUDA;
   (void)old_wup;
@@ -464,6 +495,8 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     }
     cudaMemsetAsync(b.evec, 0, (size_t)q.nvec * V * sizeof(float), s);
     cudaMemsetAsync(b.counter, 0, np * sizeof(int), s);
+    if (q.eig_mode == GPB_EIG_WARM)
+      for (int i = 0; i < 4; i++) cudaMemsetAsync(b.blk[i], 0, (size_t)kBlk * V * sizeof(float), s);
   }
   return GPB_OK;
 }
@@ -627,6 +660,212 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
   return noconv ? GPB_ERR_NOCONV : GPB_OK;
 }
 
+// ------------------------------------------------------------------------
+// Warm-startable block eigensolver: Chebyshev-filtered subspace iteration
+// (Zhou & Saad, J. Comput. Phys. 219 (2006) and Numer. Linear Algebra Appl.
+// 14 (2007)) on a block of 32 vectors.  Each outer iteration applies a
+// degree-d scaled Chebyshev filter that damps [theta_max, 2] (the spectrum of
+// the normalised Laplacian ends at 2), orthonormalises the block twice on its
+// Gram matrix (symmetric orthonormalisation, FP64 on the host) and performs a
+// Rayleigh-Ritz step; the host solves the 32 x 32 problems.  The start block
+// is the warm start; without one it is seeded noise.
+static void lowdin(const double* G, int n, double* M) {
+  // M = G^-1/2 (eigenvalues clamped), so that U M has orthonormal columns
+  std::vector<double> A(G, G + (size_t)n * n), w(n), Z((size_t)n * n);
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) A[i * n + j] = 0.5 * (G[i * n + j] + G[j * n + i]);
+  gpb::sym_eig(A.data(), n, w.data(), Z.data());
+  const double floor_ = std::max(w[n - 1], 1e-300) * 1e-15;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      double v = 0;
+      for (int k = 0; k < n; k++) v += Z[i * n + k] * Z[j * n + k] / sqrt(std::max(w[k], floor_));
+      M[i * n + j] = v;
+    }
+}
+
+static gpb_status solve_block(gpb_ctx* ctx, const Layout& L, bool have_start) {
+  Buf& b = ctx->b;
+  const gpb_params& q = ctx->prm;
+  cudaStream_t s = ctx->st;
+  const int np = (int)L.patches.size(), nt = (int)L.tiles.size(), nev = q.nvec;
+  const int nwb = (int)L.work_blk.size();
+  const int deg = std::max(2, std::min(q.cheb_degree, kMaxCheb));
+  BlkArgs a;
+  a.patches = b.patches;
+  a.tiles = b.tiles;
+  a.tile_begin = b.tile_begin;
+  a.tile_count = b.tile_count;
+  a.a_up = b.aup;
+  a.a_diag = b.adiag;
+  a.lvec = L.lvec;
+  a.coef = b.bcoef;
+  a.max_steps = kMaxCheb;
+  a.part = b.bpart;
+  a.counter = b.counter;
+  a.active = b.active;
+  a.done = b.bdone;
+  a.mat = b.bmat;
+  a.theta = b.btheta;
+  const size_t BB = (size_t)kBlk * kBlk;
+  std::vector<int> active(np, 1), done(np, 0);
+  std::vector<double> G(np * BB), M(np * BB), theta(np * (size_t)kBlk, 0.0), res(np * (size_t)kBlk);
+  std::vector<float3> coef(np * (size_t)kMaxCheb);
+  std::vector<float> evals((size_t)np * nev, 0.f);
+  std::vector<long> mv(np, 0);
+  float* X = b.blk[0];
+  float* Y = b.blk[1];
+  float* Z = b.blk[2];
+  float* AX = b.blk[3];
+  CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.bdone, done.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  if (!have_start) {
+    CK(cf_launch_init(a, nt, X, s));
+    ctx->launches++;
+  }
+  auto upload_unit = [&]() -> cudaError_t {  // coefficient (1, 0, 0) at step 0: plain SpMV
+    for (int i = 0; i < np; i++) coef[(size_t)i * kMaxCheb] = make_float3(1.f, 0.f, 0.f);
+    return cudaMemcpyAsync(b.bcoef, coef.data(), coef.size() * sizeof(float3), cudaMemcpyHostToDevice, s);
+  };
+  // orthonormalise F twice, then Rayleigh-Ritz on span(F); AF receives A F
+  auto rr = [&](float* F, float* AF) -> gpb_status {
+    for (int pass = 0; pass < 2; pass++) {
+      CK(cf_launch_gram(a, nt, F, F, b.bgram, s));
+      CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int i = 0; i < np; i++)
+        if (active[i]) {
+          lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
+          if (ctx->trace && i == 0)
+            fprintf(stderr, "[gpb] gram pass %d patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", pass, G[0],
+                    G[kBlk + 1], G[BB - 1], M[0]);
+        }
+      CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
+      ctx->launches += 2;
+    }
+    CK(upload_unit());
+    CK(cf_launch_step(a, b.work_blk, nwb, F, F, AF, 0, s));
+    CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
+    CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ctx->launches += 2;
+    for (int i = 0; i < np; i++) {
+      if (!active[i]) continue;
+      mv[i] += kBlk;
+      std::vector<double> H(BB), w(kBlk), Zm(BB);
+      for (int r = 0; r < kBlk; r++)
+        for (int c = 0; c < kBlk; c++)
+          H[r * kBlk + c] = 0.5 * (G[i * BB + r * kBlk + c] + G[i * BB + c * kBlk + r]);
+      gpb::sym_eig(H.data(), kBlk, w.data(), Zm.data());
+      for (int c = 0; c < kBlk; c++) theta[(size_t)i * kBlk + c] = w[c];
+      std::copy(Zm.begin(), Zm.end(), M.begin() + i * BB);
+    }
+    CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.btheta, theta.data(), theta.size() * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cf_launch_rotate(a, nt, F, AF, kBlk, s));
+    CK(cf_launch_resid(a, nt, F, AF, b.bres, s));
+    CK(cudaMemcpyAsync(res.data(), b.bres, res.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ctx->launches += 2;
+    return GPB_OK;
+  };
+  gpb_status st = rr(X, AX);
+  if (st != GPB_OK) return st;
+  int outer = 0;
+  float maxres = 0.f;
+  bool noconv = false;
+  for (;;) {
+    // convergence and per-patch filter coefficients
+    int nactive = 0;
+    for (int i = 0; i < np; i++) {
+      if (!active[i]) continue;
+      double worst = 0;
+      bool finite = true;
+      for (int c = 0; c < nev; c++) {
+        const double r2 = res[(size_t)i * kBlk + c];
+        if (!std::isfinite(r2)) finite = false;
+        worst = std::max(worst, sqrt(std::max(r2, 0.0)));
+      }
+      if (ctx->trace)
+        fprintf(stderr, "[gpb] block patch %d outer %d theta0 %.3e theta8 %.3e theta31 %.3e worst %.3e%s\n", i,
+                outer, theta[(size_t)i * kBlk], theta[(size_t)i * kBlk + 8], theta[(size_t)i * kBlk + kBlk - 1], worst,
+                finite ? "" : " NON-FINITE");
+      if (!finite) {
+        ctx->last_error = "non-finite residual in the block eigensolver";
+        return GPB_ERR_INTERNAL;
+      }
+      const bool conv = worst <= q.eig_tol;
+      if (conv || mv[i] + (long)(deg + 1) * kBlk > q.eig_max_matvecs) {
+        active[i] = 0;
+        done[i] = 1;
+        maxres = std::max(maxres, (float)worst);
+        if (!conv) noconv = true;
+        for (int c = 0; c < nev; c++) evals[(size_t)i * nev + c] = (float)theta[(size_t)i * kBlk + c];
+        continue;
+      }
+      nactive++;
+      // the normalised Laplacian's spectrum lies in [0, 2]: normalising the
+      // filter at 0 (not at the smallest Ritz value, which a random start
+      // puts near 1) keeps every component of the block bounded in FP32
+      const double ub = 2.0, lo0 = -1e-3, cut = theta[(size_t)i * kBlk + kBlk - 1];
+      const double e = (ub - cut) / 2, c = (ub + cut) / 2;
+      double sigma = e / (lo0 - c);
+      const double tau = 2 / sigma;
+      coef[(size_t)i * kMaxCheb] = make_float3((float)(sigma / e), (float)(-c * sigma / e), 0.f);
+      for (int k = 1; k < deg; k++) {
+        const double s2 = 1 / (tau - sigma);
+        coef[(size_t)i * kMaxCheb + k] = make_float3((float)(2 * s2 / e), (float)(-2 * c * s2 / e), (float)(-sigma * s2));
+        sigma = s2;
+      }
+      mv[i] += (long)deg * kBlk;
+    }
+    CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (nactive == 0) break;
+    CK(cudaMemcpyAsync(b.bcoef, coef.data(), coef.size() * sizeof(float3), cudaMemcpyHostToDevice, s));
+    // filter: buffers rotate X -> Y -> Z -> X ...
+    long long apx = 0;
+    for (int i = 0; i < np; i++)
+      if (active[i]) apx += L.patches[i].N;
+    float* buf[3] = {X, Y, Z};
+    int cur = 0;
+    for (int k = 0; k < deg; k++) {
+      const int nxt = (cur + 1) % 3, prv = (cur + 2) % 3;
+      // algorithmic bytes per pixel: 41 coefficients, the 32-wide rows of
+      // Y (and of the previous iterate after the first step), the output row
+      prof_begin(ctx, 0, (double)apx * (4.0 * (kUpper + 1) + 4.0 * kBlk * (k ? 3 : 2)));
+      CK(cf_launch_step(a, b.work_blk, nwb, buf[cur], buf[prv], buf[nxt], k, s));
+      prof_end(ctx);
+      cur = nxt;
+    }
+    ctx->launches += deg;
+    X = buf[cur];
+    Y = buf[(cur + 1) % 3];
+    Z = buf[(cur + 2) % 3];
+    st = rr(X, AX);
+    if (st != GPB_OK) return st;
+    outer++;
+    if (outer > 200) break;
+  }
+  CK(cudaMemcpyAsync(b.bdone, done.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cf_launch_extract(a, nt, X, b.evec, nev, s));
+  ctx->launches++;
+  CK(cudaMemcpyAsync(b.evals, evals.data(), evals.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  prof_collect(ctx);
+  ctx->evals_host = evals;
+  long tot = 0, mx = 0;
+  for (int i = 0; i < np; i++) {
+    tot += mv[i];
+    mx = std::max(mx, mv[i]);
+  }
+  ctx->stats.matvecs_total = tot;
+  ctx->stats.matvecs_max = mx;
+  ctx->stats.restarts = outer;
+  ctx->stats.max_residual = maxres;
+  return noconv ? GPB_ERR_NOCONV : GPB_OK;
+}
+
 static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const uint32_t* hs,
                             const uint32_t* const* host_in, const size_t* host_stride, const uint32_t* dev_in,
                             const size_t* dev_off, float* dev_nmax, float* dev_orient, gpb_result* host_out) {
@@ -653,6 +892,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   CK(cudaMemcpyAsync(b.work_tex, L.work_tex.data(), L.work_tex.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.work_cue, L.work_cue.data(), L.work_cue.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.work16, L.work16.data(), L.work16.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.work_blk, L.work_blk.data(), L.work_blk.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.tiles, L.tiles.data(), L.tiles.size() * sizeof(EigTile), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.tile_begin, L.tile_begin.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.tile_count, L.tile_count.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -703,7 +943,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   CK(cudaEventRecord(ctx->ev[5], s));
   ctx->launches += 10;
   // (d) eigensolver
-  gpb_status es = solve_lanczos(ctx, L);
+  gpb_status es = ctx->prm.eig_mode == GPB_EIG_WARM ? solve_block(ctx, L, false) : solve_lanczos(ctx, L);
   if (es != GPB_OK && es != GPB_ERR_NOCONV) return es;
   CK(cudaEventRecord(ctx->ev[6], s));
   // (e) sPb + gPb

@@ -1,0 +1,46 @@
+// k_block.h -- block (Chebyshev-filtered subspace iteration) kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gpb_internal.h"
+#include "k_eig.h"
+
+namespace gpb {
+
+constexpr int kBlk = 32;          // block width
+constexpr int kBlkThreads = 256;  // 64 pixels x 4 quarters per pass
+constexpr int kMaxCheb = 128;     // largest filter degree
+
+struct BlkArgs {
+  const PatchDev* patches;
+  const EigTile* tiles;
+  const int* tile_begin;
+  const int* tile_count;
+  const float* a_up;
+  const float* a_diag;
+  long long lvec;
+  const float3* coef;   // [npatch][max_steps] (alpha, beta, gamma)
+  int max_steps;
+  double* part;         // [ntiles][32*32]
+  int* counter;         // [npatch]
+  const int* active;    // [npatch]
+  const int* done;      // [npatch]
+  const double* mat;    // [npatch][32*32]
+  const double* theta;  // [npatch][32]
+};
+
+void upload_block(const HostTables& t, cudaStream_t s);
+constexpr int kStepTileH = 8, kStepTileW = 32;  // cf_step tile (work list entries)
+cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
+                           int step, cudaStream_t s);
+cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
+                           cudaStream_t s);
+cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s);
+cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const float* AX, double* out,
+                            cudaStream_t s);
+cudaError_t cf_launch_extract(const BlkArgs& a, int ntiles, const float* X, float* evec, int nvec,
+                              cudaStream_t s);
+cudaError_t cf_launch_init(const BlkArgs& a, int ntiles, float* X, cudaStream_t s);
+
+}  // namespace gpb

@@ -439,8 +439,10 @@ void build_tables(HostTables& t, int compat) {
   }
   build_ic(t);
   // sPb: 8 oriented filters at theta = o*PI/8 into slot ch_per[o]
-  // (src/spectralPb.cpp:291-322)
-  static const int chp[8] = {3, 2, 1, 0, 7, 6, 5, 4};
+  // (src/spectralPb.cpp:291-322); with the Berkeley filter the slot that
+  // aligns sPb_o with the orientation of the local cues is (4 - o) mod 8
+  // (the reference's {3,2,1,0,7,6,5,4} belongs to its own filter port)
+  static const int chp[8] = {4, 3, 2, 1, 0, 7, 6, 5};
   for (int o = 0; o < kNori; o++) {
     double f[49];
     oe_filter((kRefPi / 8) * (double)o, f);

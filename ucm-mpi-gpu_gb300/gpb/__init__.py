@@ -34,7 +34,8 @@ class Params(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("compat", ctypes.c_int), ("nvec", ctypes.c_int),
                 ("eig_tol", ctypes.c_float), ("eig_max_matvecs", ctypes.c_int),
                 ("krylov_dim", ctypes.c_int), ("krylov_keep", ctypes.c_int),
-                ("eig_mode", ctypes.c_int), ("keep_intermediates", ctypes.c_int)]
+                ("eig_mode", ctypes.c_int), ("keep_intermediates", ctypes.c_int),
+                ("cheb_degree", ctypes.c_int)]
 
 
 class Patch(ctypes.Structure):
