@@ -52,7 +52,9 @@ typedef enum {
 
 typedef enum {
   GPB_EIG_LANCZOS = 0,   /* plain cold-start thick-restart Lanczos (Krylov-Schur) */
-  GPB_EIG_WARM = 1       /* warm-started block solver, Lanczos as fallback         */
+  GPB_EIG_WARM = 1,      /* block Chebyshev-filtered solver warm-started from the
+                            2x2-aggregated (coarse) problem                       */
+  GPB_EIG_BLOCK = 2      /* the same block solver from a seeded random start      */
 } gpb_eig_mode;
 
 typedef struct {
@@ -66,6 +68,7 @@ typedef struct {
   int eig_mode;          /* gpb_eig_mode                                          */
   int keep_intermediates;/* 1: retain per-stage buffers for gpb_fetch(); 2: also counts */
   int cheb_degree;       /* Chebyshev filter degree of the block solver          */
+  float warm_tol;        /* residual at which the coarse warm-start solve stops  */
 } gpb_params;
 
 typedef struct gpb_ctx gpb_ctx;

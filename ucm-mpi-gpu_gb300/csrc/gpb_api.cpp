@@ -109,6 +109,17 @@ struct Buf {
   double* bres = nullptr; size_t c_bres = 0;
   float3* bcoef = nullptr; size_t c_bcoef = 0;
   int* bdone = nullptr; size_t c_bdone = 0;
+  // coarse level of the warm start
+  PatchDev* cpatches = nullptr; size_t c_cpatches = 0;
+  EigTile* ctiles = nullptr; size_t c_ctiles = 0;
+  int* ctile_begin = nullptr; size_t c_ctb = 0;
+  int* ctile_count = nullptr; size_t c_ctc = 0;
+  int4* cwork_blk = nullptr; size_t c_cwb = 0;
+  int4* cwork16 = nullptr; size_t c_cw16 = 0;
+  float* cwc = nullptr; size_t c_cwc = 0;
+  float* cdeg = nullptr; size_t c_cdeg = 0;
+  float* cdis = nullptr; size_t c_cdis = 0;
+  float* cblk[4] = {nullptr, nullptr, nullptr, nullptr}; size_t c_cblk[4] = {0, 0, 0, 0};
 };
 
 struct gpb_ctx {
@@ -192,6 +203,7 @@ extern "C" void gpb_default_params(gpb_params* p) {
   p->eig_mode = GPB_EIG_LANCZOS;
   p->keep_intermediates = 0;
   p->cheb_degree = 40;
+  p->warm_tol = 1e-3f;
 }
 
 extern "C" const char* gpb_status_str(gpb_status s) {
@@ -223,7 +235,8 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
   else gpb_default_params(&ctx->prm);
   gpb_params& q = ctx->prm;
   if (q.nvec < 2 || q.nvec > kMaxNvec || q.krylov_dim > kMaxKrylov || q.krylov_keep >= q.krylov_dim ||
-      q.krylov_keep < q.nvec || !(q.eig_tol > 0)) {
+      q.krylov_keep < q.nvec || !(q.eig_tol > 0) || q.eig_mode < GPB_EIG_LANCZOS || q.eig_mode > GPB_EIG_BLOCK ||
+      (q.eig_mode != GPB_EIG_LANCZOS && q.nvec > kBlk) || (q.eig_mode == GPB_EIG_WARM && !(q.warm_tol > 0))) {
     delete ctx;
     return GPB_ERR_ARG;
   }
@@ -298,7 +311,8 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
                   b.mm, b.spb, b.gpbo, b.nmax, b.orient, b.patches, b.work_tex, b.work_cue, b.work16, b.work_blk,
                   b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
                   b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
-                  b.bcoef, b.bdone};
+                  b.bcoef, b.bdone, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk,
+                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3]};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
@@ -373,7 +387,11 @@ Layout make_layout(size_t n, const uint32_t* ws, const uint32_t* hs) {
   Layout L;
   int wmax = 0;
   for (size_t i = 0; i < n; i++) wmax = std::max(wmax, (int)ws[i]);
-  const long long pad = (((long long)kStencilR * wmax + kStencilR) + 63) / 64 * 64;
+  // the gap before and after every patch: a stencil neighbour lies at most
+  // kStencilR rows + kStencilR pixels away, and a block-step tile's staged
+  // row runs kStepTileW + 2 kStencilR pixels from its left halo column
+  const long long pad =
+      (((long long)kStencilR * wmax + kStencilR + kStepTileW + 2 * kStencilR) + 63) / 64 * 64;
   long long pix = 0, vec = pad;
   for (size_t i = 0; i < n; i++) {
     PatchDev P;
@@ -412,9 +430,19 @@ Layout make_layout(size_t n, const uint32_t* ws, const uint32_t* hs) {
   return L;
 }
 
+// the 2 x 2 aggregated layout of a fine layout
+Layout make_coarse_layout(const Layout& F) {
+  std::vector<uint32_t> ws, hs;
+  for (const PatchDev& P : F.patches) {
+    ws.push_back((uint32_t)((P.W + 1) / 2));
+    hs.push_back((uint32_t)((P.H + 1) / 2));
+  }
+  return make_layout(ws.size(), ws.data(), hs.data());
+}
+
 }  // namespace
 
-static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_changed) {
+static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_changed, const Layout* C) {
   Buf& b = ctx->b;
   const gpb_params& q = ctx->prm;
   const size_t P = L.total_pix, V = L.lvec, np = L.patches.size(), nt = L.tiles.size();
@@ -468,7 +496,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
   es.push_back(grow(b.tiles, b.c_tiles, nt));
   es.push_back(grow(b.tile_begin, b.c_tb, np));
   es.push_back(grow(b.tile_count, b.c_tc, np));
-  if (q.eig_mode == GPB_EIG_WARM) {
+  if (q.eig_mode != GPB_EIG_LANCZOS) {
     for (int i = 0; i < 4; i++) es.push_back(grow(b.blk[i], b.c_blk[i], (size_t)kBlk * V));
     es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
@@ -477,6 +505,19 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     es.push_back(grow(b.bres, b.c_bres, np * kBlk));
     es.push_back(grow(b.bcoef, b.c_bcoef, np * (size_t)kMaxCheb));
     es.push_back(grow(b.bdone, b.c_bdone, np));
+  }
+  if (q.eig_mode == GPB_EIG_WARM && C) {
+    const size_t Vc = C->lvec, ntc = C->tiles.size();
+    es.push_back(grow(b.cpatches, b.c_cpatches, np));
+    es.push_back(grow(b.ctiles, b.c_ctiles, ntc));
+    es.push_back(grow(b.ctile_begin, b.c_ctb, np));
+    es.push_back(grow(b.ctile_count, b.c_ctc, np));
+    es.push_back(grow(b.cwork_blk, b.c_cwb, C->work_blk.size()));
+    es.push_back(grow(b.cwork16, b.c_cw16, C->work16.size()));
+    es.push_back(grow(b.cwc, b.c_cwc, (size_t)kCN * Vc));
+    es.push_back(grow(b.cdeg, b.c_cdeg, Vc));
+    es.push_back(grow(b.cdis, b.c_cdis, Vc));
+    for (int i = 0; i < 4; i++) es.push_back(grow(b.cblk[i], b.c_cblk[i], (size_t)kBlk * Vc));
   }
   for (cudaError_t e : es)
     if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? GPB_ERR_NOMEM : GPB_ERR_CUDA;
@@ -495,8 +536,13 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     }
     cudaMemsetAsync(b.evec, 0, (size_t)q.nvec * V * sizeof(float), s);
     cudaMemsetAsync(b.counter, 0, np * sizeof(int), s);
-    if (q.eig_mode == GPB_EIG_WARM)
+    if (q.eig_mode != GPB_EIG_LANCZOS)
       for (int i = 0; i < 4; i++) cudaMemsetAsync(b.blk[i], 0, (size_t)kBlk * V * sizeof(float), s);
+    if (q.eig_mode == GPB_EIG_WARM && C) {
+      cudaMemsetAsync(b.cwc, 0, (size_t)kCN * C->lvec * sizeof(float), s);
+      cudaMemsetAsync(b.cdis, 0, C->lvec * sizeof(float), s);
+      for (int i = 0; i < 4; i++) cudaMemsetAsync(b.cblk[i], 0, (size_t)kBlk * C->lvec * sizeof(float), s);
+    }
   }
   return GPB_OK;
 }
@@ -684,20 +730,43 @@ static void lowdin(const double* G, int n, double* M) {
     }
 }
 
-static gpb_status solve_block(gpb_ctx* ctx, const Layout& L, bool have_start) {
+// one level of the block solver: its layout, device tables, operator and
+// the four block buffers
+struct Level {
+  const Layout* L;
+  const PatchDev* patches;
+  const EigTile* tiles;
+  const int* tile_begin;
+  const int* tile_count;
+  const int4* work_blk;
+  const float* a_up;
+  const float* a_diag;
+  int coarse;
+  float* blk[4];
+};
+
+// Solves one level; on return *Xout is the buffer holding the 32 Ritz
+// vectors (ascending).  extract: write the first nvec into b.evec.
+static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, double tol, bool extract,
+                              float** Xout) {
+  const Layout& L = *lv.L;
   Buf& b = ctx->b;
   const gpb_params& q = ctx->prm;
   cudaStream_t s = ctx->st;
   const int np = (int)L.patches.size(), nt = (int)L.tiles.size(), nev = q.nvec;
   const int nwb = (int)L.work_blk.size();
-  const int deg = std::max(2, std::min(q.cheb_degree, kMaxCheb));
+  const int4* work_blk = lv.work_blk;
+  // a multiple of 3, so the three-buffer Chebyshev rotation ends where it
+  // started and every patch's vectors stay in X, converged or not
+  const int deg = std::min((std::max(3, q.cheb_degree) + 2) / 3 * 3, kMaxCheb / 3 * 3);
   BlkArgs a;
-  a.patches = b.patches;
-  a.tiles = b.tiles;
-  a.tile_begin = b.tile_begin;
-  a.tile_count = b.tile_count;
-  a.a_up = b.aup;
-  a.a_diag = b.adiag;
+  a.patches = lv.patches;
+  a.tiles = lv.tiles;
+  a.tile_begin = lv.tile_begin;
+  a.tile_count = lv.tile_count;
+  a.a_up = lv.a_up;
+  a.a_diag = lv.a_diag;
+  a.coarse = lv.coarse;
   a.lvec = L.lvec;
   a.coef = b.bcoef;
   a.max_steps = kMaxCheb;
@@ -713,10 +782,10 @@ static gpb_status solve_block(gpb_ctx* ctx, const Layout& L, bool have_start) {
   std::vector<float3> coef(np * (size_t)kMaxCheb);
   std::vector<float> evals((size_t)np * nev, 0.f);
   std::vector<long> mv(np, 0);
-  float* X = b.blk[0];
-  float* Y = b.blk[1];
-  float* Z = b.blk[2];
-  float* AX = b.blk[3];
+  float* X = lv.blk[0];
+  float* Y = lv.blk[1];
+  float* Z = lv.blk[2];
+  float* AX = lv.blk[3];
   CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.bdone, done.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
   if (!have_start) {
@@ -745,7 +814,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Layout& L, bool have_start) {
       ctx->launches += 2;
     }
     CK(upload_unit());
-    CK(cf_launch_step(a, b.work_blk, nwb, F, F, AF, 0, s));
+    CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s));
     CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
     CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -795,7 +864,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Layout& L, bool have_start) {
         ctx->last_error = "non-finite residual in the block eigensolver";
         return GPB_ERR_INTERNAL;
       }
-      const bool conv = worst <= q.eig_tol;
+      const bool conv = worst <= tol;
       if (conv || mv[i] + (long)(deg + 1) * kBlk > q.eig_max_matvecs) {
         active[i] = 0;
         done[i] = 1;
@@ -833,37 +902,84 @@ static gpb_status solve_block(gpb_ctx* ctx, const Layout& L, bool have_start) {
       const int nxt = (cur + 1) % 3, prv = (cur + 2) % 3;
       // algorithmic bytes per pixel: 41 coefficients, the 32-wide rows of
       // Y (and of the previous iterate after the first step), the output row
-      prof_begin(ctx, 0, (double)apx * (4.0 * (kUpper + 1) + 4.0 * kBlk * (k ? 3 : 2)));
-      CK(cf_launch_step(a, b.work_blk, nwb, buf[cur], buf[prv], buf[nxt], k, s));
+      prof_begin(ctx, 0, (double)apx * (4.0 * (lv.coarse ? kCN : kUpper + 1) + 4.0 * kBlk * (k ? 3 : 2)));
+      CK(cf_launch_step(a, work_blk, nwb, buf[cur], buf[prv], buf[nxt], k, s));
       prof_end(ctx);
       cur = nxt;
     }
     ctx->launches += deg;
-    X = buf[cur];
-    Y = buf[(cur + 1) % 3];
-    Z = buf[(cur + 2) % 3];
+    if (buf[cur] != X) {
+      ctx->last_error = "block filter rotation out of step";
+      return GPB_ERR_INTERNAL;
+    }
     st = rr(X, AX);
     if (st != GPB_OK) return st;
     outer++;
     if (outer > 200) break;
   }
-  CK(cudaMemcpyAsync(b.bdone, done.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
-  CK(cf_launch_extract(a, nt, X, b.evec, nev, s));
-  ctx->launches++;
-  CK(cudaMemcpyAsync(b.evals, evals.data(), evals.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  *Xout = X;
+  if (extract) {
+    CK(cudaMemcpyAsync(b.bdone, done.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cf_launch_extract(a, nt, X, b.evec, nev, s));
+    ctx->launches++;
+    CK(cudaMemcpyAsync(b.evals, evals.data(), evals.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    ctx->evals_host = evals;
+  }
   CK(cudaStreamSynchronize(s));
   prof_collect(ctx);
-  ctx->evals_host = evals;
   long tot = 0, mx = 0;
   for (int i = 0; i < np; i++) {
     tot += mv[i];
     mx = std::max(mx, mv[i]);
   }
-  ctx->stats.matvecs_total = tot;
-  ctx->stats.matvecs_max = mx;
-  ctx->stats.restarts = outer;
-  ctx->stats.max_residual = maxres;
-  return noconv ? GPB_ERR_NOCONV : GPB_OK;
+  if (ctx->trace)
+    fprintf(stderr, "[gpb] block level %s: outer %d, matvecs max %ld total %ld\n", lv.coarse ? "coarse" : "fine",
+            outer, mx, tot);
+  ctx->stats.matvecs_total += tot;
+  ctx->stats.matvecs_max += mx;
+  ctx->stats.restarts += outer;
+  if (extract) ctx->stats.max_residual = maxres;
+  return (noconv && extract) ? GPB_ERR_NOCONV : GPB_OK;
+}
+
+// warm-started block solve: the coarse (2 x 2 aggregated) problem from a
+// seeded start to a loose tolerance, its Ritz vectors prolongated to the fine
+// level as the start block, then the fine problem to the full tolerance
+static gpb_status solve_warm(gpb_ctx* ctx, const Layout& L, const Layout& Lc) {
+  Buf& b = ctx->b;
+  cudaStream_t s = ctx->st;
+  const size_t np = L.patches.size();
+  CK(cudaMemcpyAsync(b.cpatches, Lc.patches.data(), np * sizeof(PatchDev), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.ctiles, Lc.tiles.data(), Lc.tiles.size() * sizeof(EigTile), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.ctile_begin, Lc.tile_begin.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.ctile_count, Lc.tile_count.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.cwork_blk, Lc.work_blk.data(), Lc.work_blk.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(b.cwork16, Lc.work16.data(), Lc.work16.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+  CoarseArgs c;
+  c.fine = b.patches;
+  c.coarse = b.cpatches;
+  c.work = b.cwork16;
+  c.work_f = b.work16;
+  c.wsym_up = b.wup;
+  c.deg = b.deg;
+  c.lvec_f = L.lvec;
+  c.lvec_c = Lc.lvec;
+  c.wc = b.cwc;
+  c.degc = b.cdeg;
+  c.disc = b.cdis;
+  CK(cf_launch_coarsen(c, (int)Lc.work16.size(), s));
+  ctx->launches += 2;
+  Level lc = {&Lc, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk, b.cwc, nullptr, 1,
+              {b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3]}};
+  float* Xc = nullptr;
+  gpb_status st = solve_block(ctx, lc, false, ctx->prm.warm_tol, false, &Xc);
+  if (st != GPB_OK) return st;
+  CK(cf_launch_prolong(c, (int)L.work16.size(), Xc, b.blk[0], s));
+  ctx->launches++;
+  Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.aup, b.adiag, 0,
+              {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
+  float* Xf = nullptr;
+  return solve_block(ctx, lf, true, ctx->prm.eig_tol, true, &Xf);
 }
 
 static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const uint32_t* hs,
@@ -883,7 +999,10 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   std::string key;
   for (size_t i = 0; i < n; i++) key += std::to_string(ws[i]) + "x" + std::to_string(hs[i]) + ",";
   const bool changed = key != ctx->layout_key;
-  gpb_status st = ensure_buffers(ctx, L, changed);
+  Layout Lc;
+  const bool warm = ctx->prm.eig_mode == GPB_EIG_WARM;
+  if (warm) Lc = make_coarse_layout(L);
+  gpb_status st = ensure_buffers(ctx, L, changed, warm ? &Lc : nullptr);
   if (st != GPB_OK) return st;
   ctx->layout_key = key;
   const size_t np = L.patches.size();
@@ -943,7 +1062,17 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   CK(cudaEventRecord(ctx->ev[5], s));
   ctx->launches += 10;
   // (d) eigensolver
-  gpb_status es = ctx->prm.eig_mode == GPB_EIG_WARM ? solve_block(ctx, L, false) : solve_lanczos(ctx, L);
+  gpb_status es;
+  if (warm) {
+    es = solve_warm(ctx, L, Lc);
+  } else if (ctx->prm.eig_mode == GPB_EIG_BLOCK) {
+    Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.aup, b.adiag, 0,
+                {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
+    float* Xf = nullptr;
+    es = solve_block(ctx, lf, false, ctx->prm.eig_tol, true, &Xf);
+  } else {
+    es = solve_lanczos(ctx, L);
+  }
   if (es != GPB_OK && es != GPB_ERR_NOCONV) return es;
   CK(cudaEventRecord(ctx->ev[6], s));
   // (e) sPb + gPb

@@ -28,7 +28,26 @@ struct BlkArgs {
   const int* done;      // [npatch]
   const double* mat;    // [npatch][32*32]
   const double* theta;  // [npatch][32]
+  int coarse;           // 0: fine symmetric radius-5 stencil (a_up upper + a_diag)
+                        // 1: coarse full 7x7 stencil in a_up (kCN offsets)
 };
+
+// coarse level (2 x 2 aggregation)
+constexpr int kCR = 3, kCW = 2 * kCR + 1, kCN = kCW * kCW;
+struct CoarseArgs {
+  const PatchDev* fine;
+  const PatchDev* coarse;
+  const int4* work;      // coarse 16 x 16 tiles
+  const int4* work_f;    // fine 16 x 16 tiles
+  const float* wsym_up;  // fine symmetric affinities (upper offsets)
+  const float* deg;      // fine degrees
+  long long lvec_f, lvec_c;
+  float* wc;             // [kCN][lvec_c]: W_c, then A_c
+  float* degc;
+  float* disc;
+};
+cudaError_t cf_launch_coarsen(const CoarseArgs& c, int nwork_c, cudaStream_t s);
+cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc, float* xf, cudaStream_t s);
 
 void upload_block(const HostTables& t, cudaStream_t s);
 constexpr int kStepTileH = 8, kStepTileW = 32;  // cf_step tile (work list entries)

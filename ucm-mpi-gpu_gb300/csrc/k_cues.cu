@@ -117,17 +117,14 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // truncated 'same' convolution along bins (conv_in_place_1D,
-// lib_image.cc:3084-3115): out[n] = sum_j in[n + K/2 - j] k[j]
+// lib_image.cc:3084-3115): out[n] = sum_j in[n + K/2 - j] k[j] over the
+// in-range sources; kw holds this lane's kernel with out-of-range taps zeroed
 template <int K>
-__device__ __forceinline__ float bin_conv(float v, int lane, int nb, const float* k) {
+__device__ __forceinline__ float bin_conv(float v, int lane, const float (&kw)[K > 0 ? K : 1]) {
   float r = 0.f;
 #pragma unroll
-  for (int j = 0; j < K; j++) {
-    const int src = lane + K / 2 - j;
-    const float x = __shfl_sync(FULL, v, src & 31);
-    if (src >= 0 && src < nb) r = fmaf(x, k[j], r);
-  }
-  return lane < nb ? r : 0.f;
+  for (int j = 0; j < K; j++) r = fmaf(__shfl_sync(FULL, v, (lane + K / 2 - j) & 31), kw[j], r);
+  return r;
 }
 
 // one (cue, radius): counts of bin `lane` in the 16 slices -> 8 chi-squared
@@ -141,11 +138,15 @@ __device__ __forceinline__ void cue_combo(const uint8_t* hist, int c, int lane, 
   for (int q = 0; q < 16; q++)
     cs[q] = lane < nb ? (float)(hist[(c * 32 + q) * HROW + lane] + hist[(c * 32 + 16 + q) * HROW + lane]) : 0.f;
   float S[16];
+  float kw[K > 0 ? K : 1];
   if (K > 0) {
-    // mass of the smoothing kernel that stays inside [0, nb) from source bin `lane`
+    // this lane's taps (zero where the source bin is outside [0, nb), or the
+    // lane itself is) and the kernel mass that source bin `lane` keeps in range
     float m = 0.f;
 #pragma unroll
     for (int j = 0; j < K; j++) {
+      const int src = lane + K / 2 - j;
+      kw[j] = (lane < nb && src >= 0 && src < nb) ? kern[j] : 0.f;
       const int n = lane + j - K / 2;
       if (n >= 0 && n < nb) m += kern[j];
     }
@@ -160,15 +161,16 @@ __device__ __forceinline__ void cue_combo(const uint8_t* hist, int c, int lane, 
   float T = 0.f, D = 0.f;
 #pragma unroll
   for (int q = 0; q < 16; q++) {
-    ch[q] = S[q] != 0.f ? cs[q] / S[q] : 0.f;
+    ch[q] = S[q] != 0.f ? cs[q] * __frcp_rn(S[q]) : 0.f;
     T += ch[q];
     D += q < 8 ? ch[q] : -ch[q];
   }
-  if (K > 0) T = bin_conv<K>(T, lane, nb, kern);
+  if (K > 0) T = bin_conv<K>(T, lane, kw);
+  const float rT = (T != 0.f && lane < nb) ? __frcp_rn(T) : 0.f;
 #pragma unroll
   for (int o = 0; o < 8; o++) {
-    const float Do = K > 0 ? bin_conv<K>(D, lane, nb, kern) : D;
-    const float term = (Do != 0.f && lane < nb) ? Do * Do / T : 0.f;
+    const float Do = K > 0 ? bin_conv<K>(D, lane, kw) : D;
+    const float term = Do * Do * rT;
     accm[o] = fmaf(wm, term, accm[o]);
     accg[o] = fmaf(wg, term, accg[o]);
     if (raw) {

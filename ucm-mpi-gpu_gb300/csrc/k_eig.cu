@@ -178,22 +178,42 @@ __global__ void __launch_bounds__(kEigThreads) ks_orth(EigArgs a, int j, int mod
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
   const long long base = P.vec;
-  __shared__ float hs[kMaxKrylov + 1];
-  for (int i = threadIdx.x; i <= j; i += blockDim.x) hs[i] = (float)a.hbuf[(long long)t.patch * a.mp1 + i];
+  // projection coefficients as FP32 hi + lo pairs; the sum V h is formed in
+  // float-float and subtracted from w before the single rounding to FP32, so
+  // the cancellation of a converging step (|w - V h| << |w|) keeps its digits
+  __shared__ float hs[kMaxKrylov + 1], hl[kMaxKrylov + 1];
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+    const double h = a.hbuf[(long long)t.patch * a.mp1 + i];
+    hs[i] = (float)h;
+    hl[i] = (float)(h - (double)hs[i]);
+  }
   __syncthreads();
-  float wv[kEigPix];
+  float wv[kEigPix], sh[kEigPix], sl[kEigPix];
 #pragma unroll
   for (int r = 0; r < kEigPix; r++) {
     const int p = t.p0 + threadIdx.x + r * kEigThreads;
     wv[r] = p < t.p1 ? w[base + p] : 0.f;
+    sh[r] = sl[r] = 0.f;
   }
   for (int i = 0; i <= j; i++) {
-    const float h = hs[i];
+    const float h = hs[i], h2 = hl[i];
 #pragma unroll
     for (int r = 0; r < kEigPix; r++) {
       const int p = t.p0 + threadIdx.x + r * kEigThreads;
-      if (p < t.p1) wv[r] = fmaf(-h, a.V[(long long)i * a.lvec + base + p], wv[r]);
+      if (p < t.p1) {
+        const float v = a.V[(long long)i * a.lvec + base + p];
+        ff_add_prod(sh[r], sl[r], h, v);
+        sl[r] = fmaf(h2, v, sl[r]);
+      }
     }
+  }
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) {
+    // w - (sh + sl) with the subtraction of sh exact (two-difference)
+    const float d = wv[r] - sh[r];
+    const float z = d - wv[r];
+    const float e = (wv[r] - (d - z)) - (sh[r] + z);
+    wv[r] = d + (e - sl[r]);
   }
 #pragma unroll
   for (int r = 0; r < kEigPix; r++) {

@@ -19,7 +19,7 @@ LIBPATH = os.path.join(_HERE, "libgpb.so")
 
 GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT = range(6)
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
-EIG_LANCZOS, EIG_WARM = 0, 1
+EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
           "spb": 7, "cues": 8, "gpb_o": 9, "counts": 10}
 
@@ -35,7 +35,7 @@ class Params(ctypes.Structure):
                 ("eig_tol", ctypes.c_float), ("eig_max_matvecs", ctypes.c_int),
                 ("krylov_dim", ctypes.c_int), ("krylov_keep", ctypes.c_int),
                 ("eig_mode", ctypes.c_int), ("keep_intermediates", ctypes.c_int),
-                ("cheb_degree", ctypes.c_int)]
+                ("cheb_degree", ctypes.c_int), ("warm_tol", ctypes.c_float)]
 
 
 class Patch(ctypes.Structure):
