@@ -114,7 +114,7 @@ def _residuals(orc, Wd, evals, evecs):
     return np.array(out)
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_eigenvectors_residual(small, orc, mode):
     import gpb
     img, cb, _ = small
@@ -132,7 +132,7 @@ def test_eigenvectors_residual(small, orc, mode):
     ctx.close()
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_gpb_small_both_solvers(small, mode):
     import gpb
     img, cb, ref = small
@@ -199,6 +199,45 @@ def test_batch_matches_single():
         assert np.abs(or_b - or_s).max() < 1e-6
         assert np.abs(nm_b - nm_s).max() < 1e-6
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_of_different_images_per_patch_parity(orc, mode):
+    """Two unlike images in one batch converge after different numbers of
+    block iterations; each patch still matches its own oracle run."""
+    import gpb
+    from gpb import synth
+    imgs = [synth.voronoi_image(96, 128, 10, 8.0, synth.SEED_BASE + 5),
+            synth.voronoi_image(120, 100, 25, 8.0, synth.SEED_BASE + 9, lines=3)]
+    cb = synth.make_codebook(imgs[0], synth.SEED_BASE + 5, n_sample=2048)
+    ctx = gpb.Context(cb, eig_mode=mode)
+    outs = ctx.compute_batch([synth.pack_bgr(im) for im in imgs])
+    assert ctx.last_status == gpb.GPB_OK
+    for im, (nm, orr) in zip(imgs, outs):
+        ref = orc.globalpb(im, cb)
+        H, W, _ = im.shape
+        assert np.abs(nm - ref["nmax"]).max() < GPB_TOL
+        assert np.abs(orr.reshape(8, H, W) - ref["gpb_o"]).max() < GPB_TOL
+    ctx.close()
+
+
+def test_contexts_interleaved():
+    """Contexts with different codebooks and compat modes share the device's
+    constant tables; using them in turn gives each its own results."""
+    import gpb
+    from gpb import synth
+    img_a, cb_a = _img(64, 80, 6, 31)
+    img_b, cb_b = _img(72, 64, 9, 32)
+    a = gpb.Context(cb_a)
+    first = a.compute_batch([synth.pack_bgr(img_a)])[0]
+    b = gpb.Context(cb_b, compat=gpb.COMPAT_DAMASCENE)
+    only_b = b.compute_batch([synth.pack_bgr(img_b)])[0]
+    again = a.compute_batch([synth.pack_bgr(img_a)])[0]
+    b_again = b.compute_batch([synth.pack_bgr(img_b)])[0]
+    for x, y in zip(first + only_b, again + b_again):
+        assert np.array_equal(x, y)
+    a.close()
+    b.close()
 
 
 def test_errors_are_reported():

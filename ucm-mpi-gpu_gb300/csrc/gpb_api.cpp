@@ -14,6 +14,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -131,6 +133,8 @@ struct gpb_ctx {
   double* d_k32_ring = nullptr;
   int* d_ring_of = nullptr;
   int K = 0;
+  std::vector<float> cb_host;  // 13 x K, the codebook last set
+  uint64_t token = 0;          // identifies this context's constant tables
   Buf b;
   std::string last_error;
   // last call
@@ -190,6 +194,46 @@ static void prof_collect(gpb_ctx* ctx) {
     }
   }
   ctx->pn = 0;
+}
+
+// The __constant__ tables (Schmid groups, codebook, slice and stencil
+// offsets, sPb filters, the compat-mode weights) live once per device and
+// are shared by every context of the process.  Each compute call holds its
+// device's lock and reloads the tables when another context loaded the
+// bank last, so contexts with different codebooks or compat modes can be
+// used in any order from any thread.
+namespace {
+struct ConstBank {
+  std::mutex mu;
+  uint64_t owner = 0;
+};
+std::mutex g_banks_mu;
+std::map<int, ConstBank*> g_banks;
+std::atomic<uint64_t> g_next_token{1};
+
+ConstBank& bank_of(int device) {
+  std::lock_guard<std::mutex> lk(g_banks_mu);
+  ConstBank*& b = g_banks[device];
+  if (!b) b = new ConstBank();  // lives for the process
+  return *b;
+}
+}  // namespace
+
+// caller holds bank_of(ctx->device).mu; ctx's device is current
+static cudaError_t load_tables(gpb_ctx* ctx) {
+  ConstBank& bk = bank_of(ctx->device);
+  if (bk.owner == ctx->token) return cudaSuccess;
+  cudaStream_t s = ctx->st;
+  upload_front(ctx->tab, s);
+  upload_cues(ctx->tab, s);
+  upload_buildw(ctx->tab, s);
+  upload_eig(ctx->tab, s);
+  upload_spb(ctx->tab, s);
+  upload_block(ctx->tab, s);
+  if (ctx->K) upload_codebook(ctx->cb_host.data(), ctx->K, s);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) bk.owner = ctx->token;
+  return e;
 }
 
 extern "C" void gpb_default_params(gpb_params* p) {
@@ -260,12 +304,16 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
   }
   build_tables(ctx->tab, q.compat);
   cudaStream_t s = ctx->st;
-  upload_front(ctx->tab, s);
-  upload_cues(ctx->tab, s);
-  upload_buildw(ctx->tab, s);
-  upload_eig(ctx->tab, s);
-  upload_spb(ctx->tab, s);
-  upload_block(ctx->tab, s);
+  ctx->token = g_next_token++;
+  bool loaded;
+  {
+    std::lock_guard<std::mutex> lk(bank_of(ctx->device).mu);
+    loaded = load_tables(ctx) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+  }
+  if (!loaded) {
+    gpb_destroy(ctx);
+    return GPB_ERR_CUDA;
+  }
   // global tables: IC paths, FP64 ring coefficients and the offset->ring map
   size_t nic = ctx->tab.ic.size();
   std::vector<int> ring_of(2401);
@@ -304,6 +352,11 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
+  {
+    ConstBank& bk = bank_of(ctx->device);
+    std::lock_guard<std::mutex> lk(bk.mu);
+    if (bk.owner == ctx->token) bk.owner = 0;
+  }
   Buf& b = ctx->b;
   void* ptrs[] = {b.packed, b.grey, b.lab4, b.nbins, b.repair, b.repair_count, b.mpbo, b.go, b.mpb, b.raw,
                   b.wfull, b.counts, b.wup, b.aup, b.deg, b.dis, b.adiag, b.V[0], b.V[1], b.W[0], b.W[1], b.evec,
@@ -326,9 +379,12 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
 extern "C" gpb_status gpb_set_codebook(gpb_ctx* ctx, const float* cb, int K) {
   if (!ctx || !cb || K < 1 || K > kMaxCodewords) return GPB_ERR_ARG;
   cudaSetDevice(ctx->device);
-  upload_codebook(cb, K, ctx->st);
-  if (cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
+  ConstBank& bk = bank_of(ctx->device);
+  std::lock_guard<std::mutex> lk(bk.mu);
+  ctx->cb_host.assign(cb, cb + (size_t)kNschmid * K);
   ctx->K = K;
+  bk.owner = 0;  // reload everything under this context's token
+  if (load_tables(ctx) != cudaSuccess || cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
   return GPB_OK;
 }
 
@@ -991,6 +1047,8 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     if (ws[i] < (uint32_t)kMinSide || hs[i] < (uint32_t)kMinSide || ws[i] > 8192 || hs[i] > 8192)
       return GPB_ERR_ARG;
   cudaSetDevice(ctx->device);
+  std::lock_guard<std::mutex> bank_lock(bank_of(ctx->device).mu);
+  CK(load_tables(ctx));
   cudaStream_t s = ctx->st;
   Buf& b = ctx->b;
   ctx->launches = 0;

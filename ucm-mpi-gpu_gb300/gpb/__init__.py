@@ -17,7 +17,7 @@ from . import synth  # noqa: F401
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(_HERE, "libgpb.so")
 
-GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT = range(6)
+GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT, GPB_ERR_INTERNAL = range(7)
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
 EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
