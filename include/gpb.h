@@ -36,7 +36,8 @@ typedef enum {
   GPB_ERR_NOMEM = 3,     /* device or host allocation failed                     */
   GPB_ERR_NOCONV = 4,    /* the eigensolver hit its matvec cap                   */
   GPB_ERR_TIMEOUT = 5,   /* a bounded device wait gave up                        */
-  GPB_ERR_INTERNAL = 6
+  GPB_ERR_INTERNAL = 6,
+  GPB_ERR_TOO_LARGE = 7  /* image beyond gpb_texton_labels_static's fixed scratch */
 } gpb_status;
 
 typedef enum {
@@ -150,6 +151,44 @@ gpb_status gpb_compute_batch_device(gpb_ctx* ctx, size_t n, const uint32_t* widt
 gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst, size_t dst_bytes);
 
 gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st);
+
+/* Texton and Lab-bin labels of one image already on the device, computed
+ * without allocating memory, on the device or the host.  No counterpart in
+ * the reference: its texton stage (src/SPFeatures.cpp:277-360) allocates
+ * its buffers on every call, and so do gpb_compute*, which grow the
+ * context's buffers to each new batch shape.
+ *
+ * Meant for callers that cannot allocate at this point: a serving process
+ * that has handed all device memory to its own pool, or one running work on
+ * other streams that cannot take the device-wide synchronisation that
+ * cudaMalloc / cudaFree may bring.
+ *
+ * d_packed  width x height pixels, B<<16 | G<<8 | R, rows tightly packed.
+ * d_labels  width x height uint32, written as L | a<<8 | b<<16 | texton<<24
+ *           (the bytes gpb_fetch returns for GPB_STAGE_LABBINS and
+ *           GPB_STAGE_TEXTON after gpb_compute on the same image).
+ * stream    a cudaStream_t, or NULL for the context's stream; the call only
+ *           enqueues work on it.
+ * Limits    each side >= 32; width * height <= 1,048,576 (2^20) pixels, in
+ *           at most 8192 tiles of 16 x 16: a larger image returns
+ *           GPB_ERR_TOO_LARGE and launches nothing.  Both pointers 4-byte
+ *           aligned; the context needs a codebook.
+ * Scratch   one fixed array of 9,568,768 bytes in the library's device code,
+ *           one per device: the grey image, the tile list, the repair list
+ *           and its counter.  The counter must be 0 when the texton kernel
+ *           starts; the first kernel of every call writes it, so no call
+ *           depends on what an earlier one left there.
+ * First call on each device looks the array's address up
+ *           (cudaGetSymbolAddress), which may load the library's device
+ *           code: make it once before any stream capture.
+ * Overlap   all calls on one device share the one array, so two calls whose
+ *           work overlaps on the GPU (different streams or threads) race and
+ *           give wrong labels: put them on one stream, or order them with
+ *           events.  The kernels read the codebook from the device's constant
+ *           tables, which a compute call of a context with another codebook
+ *           reloads: let this call's work finish before starting one. */
+gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* d_packed,
+                                    uint32_t* d_labels, void* stream);
 
 int gpb_device_count(void);
 const char* gpb_status_str(gpb_status s);

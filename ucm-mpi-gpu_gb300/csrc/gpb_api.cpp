@@ -24,6 +24,7 @@
 #include "gpb_internal.h"
 #include "k_block.h"
 #include "k_eig.h"
+#include "k_static.h"
 #include "kernels.h"
 
 namespace gpb {
@@ -254,6 +255,7 @@ extern "C" const char* gpb_status_str(gpb_status s) {
   switch (s) {
     case GPB_OK: return "ok";
     case GPB_ERR_ARG: return "invalid argument";
+    case GPB_ERR_TOO_LARGE: return "image larger than the entry point's fixed scratch allows";
     case GPB_ERR_CUDA: return "CUDA error";
     case GPB_ERR_NOMEM: return "out of memory";
     case GPB_ERR_NOCONV: return "eigensolver did not converge";
@@ -1314,4 +1316,29 @@ extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst
       return GPB_ERR_ARG;
   }
   return e == cudaSuccess ? GPB_OK : GPB_ERR_CUDA;
+}
+
+// Texton labels of one device-resident image without allocating: the
+// kernels of the batch pipeline's texton stage on the fixed scratch area of
+// k_static.cu.  No counterpart in the reference.  Nothing here allocates,
+// on the device or the host (no error strings either: the status says it).
+extern "C" gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uint32_t height,
+                                               const uint32_t* d_packed, uint32_t* d_labels, void* stream) {
+  if (!ctx || !d_packed || !d_labels || (((uintptr_t)d_packed | (uintptr_t)d_labels) & 3u) || ctx->K == 0 ||
+      width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+    return GPB_ERR_ARG;
+  const long long N = (long long)width * height;
+  const long long tiles = (long long)((width + 15) / 16) * ((height + 15) / 16);
+  if (N > kStaticMaxPix || tiles > kStaticMaxTiles) return GPB_ERR_TOO_LARGE;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return GPB_ERR_CUDA;
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st;
+  ConstBank& bk = bank_of(ctx->device);
+  std::lock_guard<std::mutex> lk(bk.mu);
+  if (bk.owner != ctx->token) {  // this context's codebook into the constant bank first
+    if (load_tables(ctx) != cudaSuccess || cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
+  }
+  if (launch_texton_static(d_packed, (int)width, (int)height, d_labels, ctx->d_k32_ring, ctx->d_ring_of,
+                           ctx->tab.n_rings, s) != cudaSuccess)
+    return GPB_ERR_CUDA;
+  return GPB_OK;
 }

@@ -17,7 +17,9 @@ from . import synth  # noqa: F401
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(_HERE, "libgpb.so")
 
-GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT, GPB_ERR_INTERNAL = range(7)
+(GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT, GPB_ERR_INTERNAL,
+ GPB_ERR_TOO_LARGE) = range(8)
+STATIC_MAX_PIXELS = 1 << 20   # gpb_texton_labels_static's scratch limit
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
 EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
@@ -94,6 +96,8 @@ def _lib():
         L.gpb_status_str.argtypes = [c]
         L.gpb_status_str.restype = ctypes.c_char_p
         L.gpb_free.argtypes = [vp]
+        L.gpb_texton_labels_static.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
+        L.gpb_texton_labels_static.restype = c
         _L = L
     return _L
 
@@ -182,6 +186,14 @@ class Context:
         out = np.empty(shape, dtype)
         _check(_lib().gpb_fetch(self._h, STAGES[stage], patch, out.ctypes.data, out.nbytes), "gpb_fetch")
         return out
+
+    def texton_labels_static(self, width, height, d_packed, d_labels, stream=None):
+        """gpb_texton_labels_static: labels (L | a<<8 | b<<16 | texton<<24)
+        of one device-resident packed image into d_labels, with no allocation;
+        d_packed, d_labels and stream are raw device pointers / a stream
+        handle.  Only enqueues work on the stream."""
+        _check(_lib().gpb_texton_labels_static(self._h, width, height, d_packed, d_labels, stream),
+               "gpb_texton_labels_static")
 
     def stats(self):
         s = Stats()
