@@ -126,6 +126,32 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def ncu_case(eig="warm"):
+    """One batch of the workload, nothing else: the command that ncu captures
+    (a few launches of one kernel out of it).  eig="block" skips the coarse
+    level, so the first block-step launches are fine-level ones."""
+    import torch
+    import gpb
+    _, cb, _, patches = make_workload()
+    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM if eig == "warm" else gpb.EIG_BLOCK)
+    ctx.compute_batch(patches)
+    torch.cuda.synchronize()
+    print(json.dumps({"ncu_case": "done", "gpu_launches": ctx.stats()["gpu_launches"]}))
+    ctx.close()
+
+
+def traffic_per_launch(alg_bytes_per_launch):
+    """DRAM bytes of an average cf_step launch, from the committed ncu summary
+    of one full-workload launch (dram__bytes_read.sum + dram__bytes_write.sum),
+    scaled by its algorithmic bytes."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "cf_step_traffic.json")) as f:
+            t = json.load(f)
+        return alg_bytes_per_launch * t["dram_bytes"] / t["algorithmic_bytes"]
+    except Exception:
+        return None
+
+
 def run_gpu(args):
     import torch
     import gpb
@@ -226,16 +252,19 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD,
-                       "eig": "block Chebyshev-filtered subspace iteration (32 vectors, degree %d), seeded start"
-                       % ctx.params.cheb_degree,
+                       "eig": "block Chebyshev-filtered subspace iteration (32 vectors, degree %d) warm-started "
+                       "from the 2x2-aggregated problem solved to residual %.0e" % (
+                           (max(3, ctx.params.cheb_degree) + 2) // 3 * 3, ctx.params.warm_tol),
                        "eig_tol": float(ctx.params.eig_tol), "l2": "flushed (512 MB write) before each step"},
             "plain": plain,
+            "speedup_vs_plain": (value / plain["value"]) if plain else None,
             "e2e": ({"value": mpix / (e2e_ms / 1e3), "unit": "Mpix/s", "h2d_bytes_per_step": int(total * 4),
                      "d2h_bytes_per_step": int(total * 9 * 4)} if e2e_ms else None),
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None},
+                         "frac": (achieved / peak) if achieved else None,
+                         "traffic": traffic_per_launch(kb / kn) if kn else None},
             "clocks": clocks,
             "stages_ms": {k: last[k] for k in ("ms_texton", "ms_cues", "ms_nms", "ms_buildw", "ms_eig",
                                                "ms_spb")},
@@ -261,8 +290,12 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--ncu-case", action="store_true", help="one batch only (for ncu captures)")
+    ap.add_argument("--ncu-eig", default="warm", choices=["warm", "block"])
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.ncu_case:
+        ncu_case(args.ncu_eig)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -14,7 +14,10 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -123,6 +126,73 @@ struct Buf {
   float* cdeg = nullptr; size_t c_cdeg = 0;
   float* cdis = nullptr; size_t c_cdis = 0;
   float* cblk[4] = {nullptr, nullptr, nullptr, nullptr}; size_t c_cblk[4] = {0, 0, 0, 0};
+  float* afull = nullptr; size_t c_afull = 0;  // pixel-major fine stencil rows
+  int* berr = nullptr; size_t c_berr = 0;
+};
+
+// A fixed set of host threads for the per-patch dense work between device
+// phases (the 32 x 32 eigenproblems of the block solver): run(n, f) calls
+// f(0..n-1) on the workers and the calling thread and returns when all are
+// done.
+class HostPool {
+ public:
+  explicit HostPool(unsigned nthreads) {
+    for (unsigned t = 1; t < nthreads; t++) th_.emplace_back([this] { work(); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      quit_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread& t : th_) t.join();
+  }
+  void run(int n, const std::function<void(int)>& f) {
+    if (th_.empty() || n <= 1) {
+      for (int i = 0; i < n; i++) f(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      f_ = &f;
+      n_ = n;
+      next_ = 0;
+      busy_ = (int)th_.size();
+      gen_++;
+    }
+    cv_.notify_all();
+    drain();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [this] { return busy_ == 0; });
+    f_ = nullptr;
+  }
+
+ private:
+  void drain() {
+    for (int i; (i = next_.fetch_add(1)) < n_;) (*f_)(i);
+  }
+  void work() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return quit_ || gen_ != seen; });
+        if (quit_) return;
+        seen = gen_;
+      }
+      drain();
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--busy_ == 0) done_.notify_one();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* f_ = nullptr;
+  std::atomic<int> next_{0};
+  int n_ = 0, busy_ = 0;
+  uint64_t gen_ = 0;
+  bool quit_ = false;
 };
 
 struct gpb_ctx {
@@ -156,6 +226,11 @@ struct gpb_ctx {
   std::vector<int> pkind;      // 0 spmv, 1 orth
   std::vector<double> pbytes;  // algorithmic bytes of that launch
   size_t pn = 0;
+  std::unique_ptr<HostPool> pool;
+  HostPool& host_pool() {
+    if (!pool) pool.reset(new HostPool(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))));
+    return *pool;
+  }
 };
 
 // events around one eigensolver launch (kind 0 = SpMV, 1 = CGS pass)
@@ -367,7 +442,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
                   b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
                   b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
                   b.bcoef, b.bdone, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk,
-                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3]};
+                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
@@ -556,6 +631,8 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
   es.push_back(grow(b.tile_count, b.c_tc, np));
   if (q.eig_mode != GPB_EIG_LANCZOS) {
     for (int i = 0; i < 4; i++) es.push_back(grow(b.blk[i], b.c_blk[i], (size_t)kBlk * V));
+    es.push_back(grow(b.afull, b.c_afull, (size_t)kFullNC * V));
+    es.push_back(grow(b.berr, b.c_berr, 1));
     es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
     es.push_back(grow(b.bmat, b.c_bmat, np * kBlk * kBlk));
@@ -572,7 +649,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     es.push_back(grow(b.ctile_count, b.c_ctc, np));
     es.push_back(grow(b.cwork_blk, b.c_cwb, C->work_blk.size()));
     es.push_back(grow(b.cwork16, b.c_cw16, C->work16.size()));
-    es.push_back(grow(b.cwc, b.c_cwc, (size_t)kCN * Vc));
+    es.push_back(grow(b.cwc, b.c_cwc, (size_t)kCoarseNC * Vc));
     es.push_back(grow(b.cdeg, b.c_cdeg, Vc));
     es.push_back(grow(b.cdis, b.c_cdis, Vc));
     for (int i = 0; i < 4; i++) es.push_back(grow(b.cblk[i], b.c_cblk[i], (size_t)kBlk * Vc));
@@ -594,10 +671,12 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     }
     cudaMemsetAsync(b.evec, 0, (size_t)q.nvec * V * sizeof(float), s);
     cudaMemsetAsync(b.counter, 0, np * sizeof(int), s);
-    if (q.eig_mode != GPB_EIG_LANCZOS)
+    if (q.eig_mode != GPB_EIG_LANCZOS) {
       for (int i = 0; i < 4; i++) cudaMemsetAsync(b.blk[i], 0, (size_t)kBlk * V * sizeof(float), s);
+      cudaMemsetAsync(b.afull, 0, (size_t)kFullNC * V * sizeof(float), s);
+    }
     if (q.eig_mode == GPB_EIG_WARM && C) {
-      cudaMemsetAsync(b.cwc, 0, (size_t)kCN * C->lvec * sizeof(float), s);
+      cudaMemsetAsync(b.cwc, 0, (size_t)kCoarseNC * C->lvec * sizeof(float), s);
       cudaMemsetAsync(b.cdis, 0, C->lvec * sizeof(float), s);
       for (int i = 0; i < 4; i++) cudaMemsetAsync(b.cblk[i], 0, (size_t)kBlk * C->lvec * sizeof(float), s);
     }
@@ -797,8 +876,7 @@ struct Level {
   const int* tile_begin;
   const int* tile_count;
   const int4* work_blk;
-  const float* a_up;
-  const float* a_diag;
+  const float* afull;  // pixel-major stencil rows of the level's operator
   int coarse;
   float* blk[4];
 };
@@ -822,8 +900,10 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   a.tiles = lv.tiles;
   a.tile_begin = lv.tile_begin;
   a.tile_count = lv.tile_count;
-  a.a_up = lv.a_up;
-  a.a_diag = lv.a_diag;
+  a.a_up = nullptr;
+  a.a_diag = nullptr;
+  a.afull = lv.afull;
+  a.err = b.berr;
   a.coarse = lv.coarse;
   a.lvec = L.lvec;
   a.coef = b.bcoef;
@@ -860,13 +940,12 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
       CK(cf_launch_gram(a, nt, F, F, b.bgram, s));
       CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
-      for (int i = 0; i < np; i++)
-        if (active[i]) {
-          lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
-          if (ctx->trace && i == 0)
-            fprintf(stderr, "[gpb] gram pass %d patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", pass, G[0],
-                    G[kBlk + 1], G[BB - 1], M[0]);
-        }
+      ctx->host_pool().run(np, [&](int i) {
+        if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
+      });
+      if (ctx->trace && active[0])
+        fprintf(stderr, "[gpb] gram pass %d patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", pass, G[0],
+                G[kBlk + 1], G[BB - 1], M[0]);
       CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
       CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
       ctx->launches += 2;
@@ -877,8 +956,8 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     ctx->launches += 2;
-    for (int i = 0; i < np; i++) {
-      if (!active[i]) continue;
+    ctx->host_pool().run(np, [&](int i) {
+      if (!active[i]) return;
       mv[i] += kBlk;
       std::vector<double> H(BB), w(kBlk), Zm(BB);
       for (int r = 0; r < kBlk; r++)
@@ -887,7 +966,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
       gpb::sym_eig(H.data(), kBlk, w.data(), Zm.data());
       for (int c = 0; c < kBlk; c++) theta[(size_t)i * kBlk + c] = w[c];
       std::copy(Zm.begin(), Zm.end(), M.begin() + i * BB);
-    }
+    });
     CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.btheta, theta.data(), theta.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cf_launch_rotate(a, nt, F, AF, kBlk, s));
@@ -958,9 +1037,10 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     int cur = 0;
     for (int k = 0; k < deg; k++) {
       const int nxt = (cur + 1) % 3, prv = (cur + 2) % 3;
-      // algorithmic bytes per pixel: 41 coefficients, the 32-wide rows of
-      // Y (and of the previous iterate after the first step), the output row
-      prof_begin(ctx, 0, (double)apx * (4.0 * (lv.coarse ? kCN : kUpper + 1) + 4.0 * kBlk * (k ? 3 : 2)));
+      // algorithmic bytes per pixel: the stencil row's coefficients, the
+      // 32-wide rows of Y (and of the previous iterate after the first
+      // step), the output row
+      prof_begin(ctx, 0, (double)apx * (4.0 * (lv.coarse ? kCN : kStencilN) + 4.0 * kBlk * (k ? 3 : 2)));
       CK(cf_launch_step(a, work_blk, nwb, buf[cur], buf[prv], buf[nxt], k, s));
       prof_end(ctx);
       cur = nxt;
@@ -1027,14 +1107,14 @@ static gpb_status solve_warm(gpb_ctx* ctx, const Layout& L, const Layout& Lc) {
   c.disc = b.cdis;
   CK(cf_launch_coarsen(c, (int)Lc.work16.size(), s));
   ctx->launches += 2;
-  Level lc = {&Lc, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk, b.cwc, nullptr, 1,
+  Level lc = {&Lc, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk, b.cwc, 1,
               {b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3]}};
   float* Xc = nullptr;
   gpb_status st = solve_block(ctx, lc, false, ctx->prm.warm_tol, false, &Xc);
   if (st != GPB_OK) return st;
   CK(cf_launch_prolong(c, (int)L.work16.size(), Xc, b.blk[0], s));
   ctx->launches++;
-  Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.aup, b.adiag, 0,
+  Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.afull, 0,
               {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
   float* Xf = nullptr;
   return solve_block(ctx, lf, true, ctx->prm.eig_tol, true, &Xf);
@@ -1119,6 +1199,11 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   CK(launch_buildw(b.patches, b.work16, (int)L.work16.size(), b.mpb, ctx->d_ic, b.wup, b.deg, L.lvec, s));
   CK(launch_scale(b.patches, b.work16, (int)L.work16.size(), b.wup, b.deg, b.aup, b.adiag, b.dis, L.lvec,
                   ctx->prm.keep_intermediates ? b.wfull : nullptr, s));
+  if (ctx->prm.eig_mode != GPB_EIG_LANCZOS) {
+    CK(cf_launch_full(b.patches, b.work16, (int)L.work16.size(), b.aup, b.adiag, L.lvec, b.afull, s));
+    CK(cudaMemsetAsync(b.berr, 0, sizeof(int), s));
+    ctx->launches++;
+  }
   CK(cudaEventRecord(ctx->ev[5], s));
   ctx->launches += 10;
   // (d) eigensolver
@@ -1126,7 +1211,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   if (warm) {
     es = solve_warm(ctx, L, Lc);
   } else if (ctx->prm.eig_mode == GPB_EIG_BLOCK) {
-    Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.aup, b.adiag, 0,
+    Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.afull, 0,
                 {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
     float* Xf = nullptr;
     es = solve_block(ctx, lf, false, ctx->prm.eig_tol, true, &Xf);
@@ -1134,6 +1219,15 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     es = solve_lanczos(ctx, L);
   }
   if (es != GPB_OK && es != GPB_ERR_NOCONV) return es;
+  if (ctx->prm.eig_mode != GPB_EIG_LANCZOS) {
+    int berr = 0;
+    CK(cudaMemcpyAsync(&berr, b.berr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (berr) {
+      ctx->last_error = "a block-step tile gave up waiting for its staged data";
+      return GPB_ERR_TIMEOUT;
+    }
+  }
   CK(cudaEventRecord(ctx->ev[6], s));
   // (e) sPb + gPb
   float* o_nmax = dev_nmax ? dev_nmax : b.nmax;

@@ -3,9 +3,8 @@
 //
 // A block of kBlk = 32 vectors is stored pixel-major ([vec][32] floats) in the
 // padded vector layout, so every stencil neighbour of a pixel is one
-// contiguous 128-byte row.  Four threads own a pixel, eight columns each
-// (two float4), so a warp reads whole rows and the stencil coefficient is
-// loaded once per thread.
+// contiguous 128-byte row; the operator of the block kernels is stored
+// pixel-major too, one full stencil row per pixel (cf_full).
 //
 //   cf_step    Y' = alpha (A Y) + beta Y + gamma X   (scaled Chebyshev
 //              recurrence, Zhou & Saad 2007; with alpha=1, beta=gamma=0 it
@@ -20,12 +19,31 @@
 // src/spectralPb.cpp:221-245 define the problem; the block method is this
 // project's own.
 #include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
 
 #include "gpb_internal.h"
 #include "k_block.h"
 #include "k_eig.h"
 
 namespace gpb {
+
+// radius-5 disk offsets in scanline order (dy, then dx, ascending): the
+// upper half -- after the centre -- numbered k = 0..39 as the a_up planes
+__host__ __device__ constexpr bool in_disk(int dy, int dx) {
+  return dy * dy + dx * dx <= kStencilR * kStencilR;
+}
+__host__ __device__ constexpr int disk_half_width(int dy) {  // floor(sqrt(25 - dy^2))
+  return dy < 0 ? disk_half_width(-dy) : dy == 0 ? 5 : dy <= 3 ? 4 : dy == 4 ? 3 : 0;
+}
+__host__ __device__ constexpr int upper_rows_before(int dy) {  // offsets in rows 1..dy-1
+  return dy <= 1 ? 0 : upper_rows_before(dy - 1) + 2 * disk_half_width(dy - 1) + 1;
+}
+__host__ __device__ constexpr int upper_k(int dy, int dx) {
+  return dy == 0 ? dx - 1 : kStencilR + upper_rows_before(dy) + dx + disk_half_width(dy);
+}
+static_assert(upper_k(0, 1) == 0 && upper_k(1, -4) == 5 && upper_k(5, 0) == kUpper - 1, "upper offset numbering");
+
 
 __constant__ int c_bup_dy[kUpper], c_bup_dx[kUpper];
 
@@ -34,6 +52,10 @@ void upload_block(const HostTables& t, cudaStream_t s) {
   for (int j = 0; j < kUpper; j++) {
     dy[j] = t.sdy[kStencilN / 2 + 1 + j];
     dx[j] = t.sdx[kStencilN / 2 + 1 + j];
+    if (upper_k(dy[j], dx[j]) != j) {  // cf_step numbers the offsets at compile time
+      fprintf(stderr, "gpb: stencil offset table out of scanline order at %d\n", j);
+      abort();
+    }
   }
   cudaMemcpyToSymbolAsync(c_bup_dy, dy, sizeof(dy), 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_bup_dx, dx, sizeof(dx), 0, cudaMemcpyHostToDevice, s);
@@ -49,101 +71,217 @@ __device__ __forceinline__ void fma4(float4& acc, float a, const float4& x) {
 }
 
 // ------------------------------------------------------------ Chebyshev step
-// One CTA owns an 8 x 32 pixel tile; the 32-wide rows of Y for the tile and a
-// 5-pixel halo are staged transposed in shared memory (column-major planes,
-// odd plane stride, so a warp reading 32 neighbouring pixels of one column
-// hits 32 banks).  Lane = pixel, warp = tile row: each lane keeps its pixel's
-// 32 outputs in registers, loads each stencil coefficient once (coalesced
-// across the warp) and streams the neighbour's 32 values from shared memory.
-constexpr int ST_H = 8, ST_W = 32, ST_R = kStencilR;
-constexpr int ST_PH = ST_H + 2 * ST_R, ST_PW = ST_W + 2 * ST_R;
-constexpr int ST_PLANE = ST_PH * ST_PW + 1;  // 757: odd, conflict-free transposes
-constexpr size_t kStepSmem = (size_t)kBlk * ST_PLANE * sizeof(float);
+// One CTA owns a kStepTileH x kStepTileW (8 x 16) pixel tile.  One thread
+// issues bulk asynchronous copies (cp.async.bulk, completion counted on an
+// mbarrier) of the tile's Y rows with an R-pixel halo -- each a contiguous
+// (16 + 2R) x 128-byte run of the pixel-major block -- and of the tile's
+// coefficient rows (pixel-major, one full stencil row per pixel).  Then lane
+// = block column: a warp computes a 4 x 4 pixel block for all 32 columns, so
+// a staged value (one conflict-free 128-byte shared row per warp) feeds up
+// to 16 pixels and one broadcast 16-byte load brings four coefficients of a
+// pixel.  About one shared-memory wavefront per output instead of 2.6.
 
-__global__ void __launch_bounds__(ST_H * 32, 2) cf_step(BlkArgs a, const int4* __restrict__ work,
-                                                     const float* __restrict__ Y, const float* __restrict__ X,
-                                                     float* __restrict__ out, int step) {
-  extern __shared__ float yt[];  // [32][ST_PLANE]
-  const int4 w = work[blockIdx.x];  // (patch, y0, x0, -)
+// the radius-5 disk of the fine level (81 offsets in scanline order, rows
+// padded to 84 floats = 21 x 16 bytes) and the 7 x 7 square of the coarse one
+template <int NCOEF_, int R_>
+struct StencilBase {
+  static constexpr int R = R_, NC = NCOEF_;
+};
+struct DiskStencil : StencilBase<84, kStencilR> {
+  static constexpr int N = kStencilN;
+  __host__ __device__ static constexpr bool in(int dy, int dx) { return in_disk(dy, dx); }
+  __host__ __device__ static constexpr int rows_before(int dy) {  // offsets in rows -R..dy-1
+    return dy <= -R ? 0 : rows_before(dy - 1) + 2 * disk_half_width(dy - 1) + 1;
+  }
+  __host__ __device__ static constexpr int index(int dy, int dx) { return rows_before(dy) + dx + disk_half_width(dy); }
+};
+struct SquareStencil : StencilBase<52, kCR> {
+  static constexpr int N = kCN;
+  __host__ __device__ static constexpr bool in(int dy, int dx) {
+    return dy >= -R && dy <= R && dx >= -R && dx <= R;
+  }
+  __host__ __device__ static constexpr int index(int dy, int dx) { return (dy + R) * (2 * R + 1) + dx + R; }
+};
+static_assert(DiskStencil::index(0, 0) == kStencilN / 2 && DiskStencil::index(kStencilR, 0) == kStencilN - 1,
+              "disk numbering");
+static_assert(SquareStencil::index(kCR, kCR) == kCN - 1, "square numbering");
+static_assert(DiskStencil::NC == kFullNC && SquareStencil::NC == kCoarseNC, "row widths");
+
+constexpr int ST_TY = kStepTileH, ST_TX = kStepTileW, ST_B = 4;  // tile and per-warp block
+static_assert((ST_TY / ST_B) * (ST_TX / ST_B) == 8, "8 warps cover the tile");
+
+template <class S>
+struct StepSmem {
+  static constexpr int PH = ST_TY + 2 * S::R, PW = ST_TX + 2 * S::R;
+  static constexpr size_t y_bytes = (size_t)PH * PW * kBlk * sizeof(float);
+  static constexpr size_t c_bytes = (size_t)ST_TY * ST_TX * S::NC * sizeof(float);
+  static constexpr size_t bytes = y_bytes + c_bytes + 16;  // + the mbarrier
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared bulk copy: both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+// polls of the tile's barrier before a CTA gives up (each poll may suspend
+// the thread for a short hardware-defined time; the copies take microseconds)
+constexpr int kBarSpin = 1 << 20;
+
+template <int K>
+__device__ __forceinline__ float f4get(const float4& v) {
+  if constexpr (K == 0) return v.x;
+  else if constexpr (K == 1) return v.y;
+  else if constexpr (K == 2) return v.z;
+  else return v.w;
+}
+
+// one staged position (RY, DX) relative to the warp's block origin: the value
+// of this lane's column there, times the coefficient of every block pixel
+// whose stencil covers it
+template <class S, int RY, int DX, int I>
+__device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float v, float4 (&cw)[16], float (&acc)[16]) {
+  if constexpr (I < ST_B * ST_B) {
+    constexpr int bi = I / ST_B, bj = I % ST_B;
+    if constexpr (S::in(RY - bi, DX - bj)) {
+      constexpr int idx = S::index(RY - bi, DX - bj);
+      // a pixel meets its offsets in scanline order, so chunk idx/4 is
+      // first needed at idx % 4 == 0
+      if constexpr (idx % 4 == 0) cw[I] = *(const float4*)(cs + (bi * ST_TX + bj) * S::NC + idx);
+      acc[I] = fmaf(f4get<idx % 4>(cw[I]), v, acc[I]);
+    }
+    step_pixels<S, RY, DX, I + 1>(cs, v, cw, acc);
+  }
+}
+
+template <class S, int P>
+__device__ __forceinline__ void step_positions(const float* __restrict__ ys, const float* __restrict__ cs,
+                                               float4 (&cw)[16], float (&acc)[16]) {
+  constexpr int NX = ST_B + 2 * S::R;
+  if constexpr (P < NX * NX) {
+    constexpr int RY = P / NX - S::R, DX = P % NX - S::R;
+    constexpr bool any = [] {
+      for (int i = 0; i < ST_B; i++)
+        for (int j = 0; j < ST_B; j++)
+          if (S::in(RY - i, DX - j)) return true;
+      return false;
+    }();
+    if constexpr (any) {
+      const float v = ys[((RY + S::R) * StepSmem<S>::PW + (DX + S::R)) * kBlk];
+      step_pixels<S, RY, DX, 0>(cs, v, cw, acc);
+    }
+    step_positions<S, P + 1>(ys, cs, cw, acc);
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(256, 2) cf_step_t(BlkArgs a, const int4* __restrict__ work,
+                                                    const float* __restrict__ Y, const float* __restrict__ X,
+                                                    float* __restrict__ out, int step) {
+  using SM = StepSmem<S>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float* ys = (float*)smem;                     // [PH][PW][32]
+  float* cs = (float*)(smem + SM::y_bytes);     // [TY * TX][NC]
+  uint64_t* bar = (uint64_t*)(smem + SM::y_bytes + SM::c_bytes);
+  const int4 w = work[blockIdx.x];              // (patch, y0, x0, -)
   if (!a.active[w.x]) return;
   const PatchDev P = a.patches[w.x];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // stage rows (y0-5 .. y0+12, x0-5 .. x0+36): each tile row is one
-  // contiguous run of 42 x 128 bytes; threads fetch float4s, eight in flight
-  // per thread, and scatter them into the transposed planes
-  {
-    constexpr int F4_PER_ROW = kBlk / 4;                 // 8 float4 per pixel
-    constexpr int F4_PER_TROW = ST_PW * F4_PER_ROW;      // 336 per tile row
-    constexpr int TOTAL = ST_PH * F4_PER_TROW;           // 6048
-    constexpr int PER_THREAD = (TOTAL + ST_H * 32 - 1) / (ST_H * 32);
-    float4 v[PER_THREAD];
-#pragma unroll
-    for (int i = 0; i < PER_THREAD; i++) {
-      const int f = threadIdx.x + i * ST_H * 32;
-      const int ty = f / F4_PER_TROW, rem = f % F4_PER_TROW;
-      // rows below the patch's last row + radius feed no in-patch pixel
-      v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (f < TOTAL && w.y - ST_R + ty < P.H + ST_R) {
-        const long long q0 = P.vec + (long long)(w.y - ST_R + ty) * P.W + (w.z - ST_R);
-        v[i] = ((const float4*)(Y + q0 * kBlk))[rem];
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < PER_THREAD; i++) {
-      const int f = threadIdx.x + i * ST_H * 32;
-      if (f < TOTAL) {
-        const int ty = f / F4_PER_TROW, rem = f % F4_PER_TROW;
-        const int tx = rem / F4_PER_ROW, c = (rem % F4_PER_ROW) * 4;
-        const int r = ty * ST_PW + tx;
-        yt[(c + 0) * ST_PLANE + r] = v[i].x;
-        yt[(c + 1) * ST_PLANE + r] = v[i].y;
-        yt[(c + 2) * ST_PLANE + r] = v[i].z;
-        yt[(c + 3) * ST_PLANE + r] = v[i].w;
-      }
-    }
-  }
+  const int ylast = min(w.y + ST_TY - 1, P.H - 1);  // rows past it feed no in-patch pixel
+  if (threadIdx.x == 0) mbar_init(bar, 1);
   __syncthreads();
-  const int y = w.y + warp, x = w.z + lane;
-  if (y >= P.H || x >= P.W) return;
-  const long long q = P.vec + (long long)y * P.W + x;
+  if (threadIdx.x == 0) {
+    const int ny = ylast - w.y + 1 + 2 * S::R, nc = ylast - w.y + 1;
+    constexpr uint32_t yrow = SM::PW * kBlk * sizeof(float), crow = ST_TX * S::NC * sizeof(float);
+    mbar_expect_tx(bar, (uint32_t)ny * yrow + (uint32_t)nc * crow);
+    for (int r = 0; r < ny; r++)
+      bulk_g2s(ys + (size_t)r * SM::PW * kBlk,
+               Y + (P.vec + (long long)(w.y - S::R + r) * P.W + (w.z - S::R)) * kBlk, yrow, bar);
+    for (int r = 0; r < nc; r++)
+      bulk_g2s(cs + (size_t)r * ST_TX * S::NC, a.afull + (P.vec + (long long)(w.y + r) * P.W + w.z) * S::NC, crow,
+               bar);
+  }
+  bool ready = false;
+  for (int it = 0; it < kBarSpin; it++)
+    if (mbar_try_wait(bar, 0)) {
+      ready = true;
+      break;
+    }
+  if (!ready) {  // record it, let the copies land, leave the tile undone
+    if (threadIdx.x == 0) atomicExch(a.err, 1);
+    for (int it = 0; it < kBarSpin && !mbar_try_wait(bar, 0); it++) {
+    }
+    return;
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int by = (warp / (ST_TX / ST_B)) * ST_B, bx = (warp % (ST_TX / ST_B)) * ST_B;
+  float acc[16];
+  float4 cw[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) acc[i] = 0.f;
+  step_positions<S, 0>(ys + (by * SM::PW + bx) * kBlk + lane, cs + (by * ST_TX + bx) * S::NC, cw, acc);
   const float3 co = a.coef[(long long)w.x * a.max_steps + step];
-  float acc[kBlk];
-  const int ctr = (warp + ST_R) * ST_PW + (lane + ST_R);
-  {
-    const float d = a.a_diag[q];
 #pragma unroll
-    for (int c = 0; c < kBlk; c++) acc[c] = d * yt[c * ST_PLANE + ctr];
+  for (int i = 0; i < 16; i++) {
+    const int y = w.y + by + i / ST_B, x = w.z + bx + i % ST_B;
+    if (y >= P.H || x >= P.W) continue;
+    const long long q = P.vec + (long long)y * P.W + x;
+    const float yc = ys[((by + i / ST_B + S::R) * SM::PW + bx + i % ST_B + S::R) * kBlk + lane];
+    float r = co.x * acc[i] + co.y * yc;
+    if (co.z != 0.f) r = fmaf(co.z, X[q * kBlk + lane], r);
+    out[q * kBlk + lane] = r;
   }
-#pragma unroll 1
-  for (int k = 0; k < kUpper; k++) {
-    const int dy = c_bup_dy[k], dx = c_bup_dx[k];
-    const long long off = (long long)dy * P.W + dx;
-    const float* au = a.a_up + (long long)k * a.lvec;
-    const float cu = au[q], cl = au[q - off];
-    const int su = ctr + dy * ST_PW + dx, sl = ctr - dy * ST_PW - dx;
-#pragma unroll
-    for (int c = 0; c < kBlk; c++) {
-      acc[c] = fmaf(cu, yt[c * ST_PLANE + su], acc[c]);
-      acc[c] = fmaf(cl, yt[c * ST_PLANE + sl], acc[c]);
+}
+
+// pixel-major full stencil rows of the fine operator from its symmetric
+// storage: row p holds A(p, p + off_e) for the 81 offsets e in scanline
+// order (0 where the neighbour is outside the patch), then 3 zeros
+__global__ void __launch_bounds__(256) cf_full(const PatchDev* __restrict__ patches, const int4* __restrict__ work,
+                                               const float* __restrict__ a_up, const float* __restrict__ a_diag,
+                                               long long lvec, float* __restrict__ afull) {
+  const int4 w = work[blockIdx.x];  // 16 x 16 tile
+  const PatchDev P = patches[w.x];
+  constexpr int NC = DiskStencil::NC;
+  for (int item = threadIdx.x; item < 256 * NC; item += blockDim.x) {
+    const int t = item / NC, e = item % NC;
+    const int y = w.y + t / 16, x = w.z + t % 16;
+    if (y >= P.H || x >= P.W) continue;
+    const long long p = P.vec + (long long)y * P.W + x;
+    float v = 0.f;
+    if (e < kStencilN) {
+      const int ctr = kStencilN / 2;
+      int dy, dx, k;
+      if (e == ctr) {
+        v = a_diag[p];
+      } else {
+        // upper offsets are c_bup[e - 41]; the disk is point-symmetric, so
+        // lower offset e mirrors upper offset 80 - e
+        k = e > ctr ? e - ctr - 1 : kStencilN - 1 - e - ctr - 1;
+        dy = e > ctr ? c_bup_dy[k] : -c_bup_dy[k];
+        dx = e > ctr ? c_bup_dx[k] : -c_bup_dx[k];
+        const int yy = y + dy, xx = x + dx;
+        if (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W)
+          v = e > ctr ? a_up[(long long)k * lvec + p] : a_up[(long long)k * lvec + p + (long long)dy * P.W + dx];
+      }
     }
-  }
-  float4* oq = (float4*)(out + q * kBlk);
-  const float4* xq = (const float4*)(X + q * kBlk);
-#pragma unroll
-  for (int c4 = 0; c4 < kBlk / 4; c4++) {
-    float4 r;
-    r.x = co.x * acc[4 * c4 + 0] + co.y * yt[(4 * c4 + 0) * ST_PLANE + ctr];
-    r.y = co.x * acc[4 * c4 + 1] + co.y * yt[(4 * c4 + 1) * ST_PLANE + ctr];
-    r.z = co.x * acc[4 * c4 + 2] + co.y * yt[(4 * c4 + 2) * ST_PLANE + ctr];
-    r.w = co.x * acc[4 * c4 + 3] + co.y * yt[(4 * c4 + 3) * ST_PLANE + ctr];
-    if (co.z != 0.f) {
-      const float4 xv = xq[c4];
-      r.x = fmaf(co.z, xv.x, r.x);
-      r.y = fmaf(co.z, xv.y, r.y);
-      r.z = fmaf(co.z, xv.z, r.z);
-      r.w = fmaf(co.z, xv.w, r.w);
-    }
-    oq[c4] = r;
+    afull[p * NC + e] = v;
   }
 }
 
@@ -355,8 +493,9 @@ __global__ void __launch_bounds__(256) cf_coarsen(CoarseArgs c) {
       }
     }
   const long long P = C.vec + (long long)Y * C.W + X;
+  constexpr int NC = SquareStencil::NC;
 #pragma unroll
-  for (int k = 0; k < kCN; k++) c.wc[(long long)k * c.lvec_c + P] = acc[k];
+  for (int k = 0; k < NC; k++) c.wc[P * NC + k] = k < kCN ? acc[k] : 0.f;
   c.degc[P] = (float)deg;
   c.disc[P] = (float)(1.0 / sqrt(deg));
 }
@@ -369,94 +508,15 @@ __global__ void __launch_bounds__(256) cf_coarse_norm(CoarseArgs c) {
   if (Y >= C.H || X >= C.W) return;
   const long long P = C.vec + (long long)Y * C.W + X;
   const float dp = c.disc[P];
+  constexpr int NC = SquareStencil::NC;
   for (int k = 0; k < kCN; k++) {
     const int dY = k / kCW - kCR, dX = k % kCW - kCR;
     const int YY = Y + dY, XX = X + dX;
     float v = 0.f;
     if (YY >= 0 && YY < C.H && XX >= 0 && XX < C.W)
-      v = -c.wc[(long long)k * c.lvec_c + P] * dp * c.disc[C.vec + (long long)YY * C.W + XX];
+      v = -c.wc[P * NC + k] * dp * c.disc[C.vec + (long long)YY * C.W + XX];
     if (k == kCR * kCW + kCR) v += 1.f;
-    c.wc[(long long)k * c.lvec_c + P] = v;
-  }
-}
-
-// coarse Chebyshev step: as cf_step, full 7 x 7 stencil, halo 3
-constexpr int SC_PH = ST_H + 2 * kCR, SC_PW = ST_W + 2 * kCR;
-constexpr int SC_PLANE = SC_PH * SC_PW + 1;  // 533: odd
-constexpr size_t kStepCSmem = (size_t)kBlk * SC_PLANE * sizeof(float);
-
-__global__ void __launch_bounds__(ST_H * 32, 2) cf_step_c(BlkArgs a, const int4* __restrict__ work,
-                                                          const float* __restrict__ Y, const float* __restrict__ X,
-                                                          float* __restrict__ out, int step) {
-  extern __shared__ float yt[];
-  const int4 w = work[blockIdx.x];
-  if (!a.active[w.x]) return;
-  const PatchDev P = a.patches[w.x];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  {
-    constexpr int F4_PER_ROW = kBlk / 4;
-    constexpr int F4_PER_TROW = SC_PW * F4_PER_ROW;
-    constexpr int TOTAL = SC_PH * F4_PER_TROW;
-    constexpr int PER_THREAD = (TOTAL + ST_H * 32 - 1) / (ST_H * 32);
-    float4 v[PER_THREAD];
-#pragma unroll
-    for (int i = 0; i < PER_THREAD; i++) {
-      const int f = threadIdx.x + i * ST_H * 32;
-      const int ty = f / F4_PER_TROW, rem = f % F4_PER_TROW;
-      v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (f < TOTAL && w.y - kCR + ty < P.H + kCR) {
-        const long long q0 = P.vec + (long long)(w.y - kCR + ty) * P.W + (w.z - kCR);
-        v[i] = ((const float4*)(Y + q0 * kBlk))[rem];
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < PER_THREAD; i++) {
-      const int f = threadIdx.x + i * ST_H * 32;
-      if (f < TOTAL) {
-        const int ty = f / F4_PER_TROW, rem = f % F4_PER_TROW;
-        const int tx = rem / F4_PER_ROW, c = (rem % F4_PER_ROW) * 4;
-        const int r = ty * SC_PW + tx;
-        yt[(c + 0) * SC_PLANE + r] = v[i].x;
-        yt[(c + 1) * SC_PLANE + r] = v[i].y;
-        yt[(c + 2) * SC_PLANE + r] = v[i].z;
-        yt[(c + 3) * SC_PLANE + r] = v[i].w;
-      }
-    }
-  }
-  __syncthreads();
-  const int y = w.y + warp, x = w.z + lane;
-  if (y >= P.H || x >= P.W) return;
-  const long long q = P.vec + (long long)y * P.W + x;
-  const float3 co = a.coef[(long long)w.x * a.max_steps + step];
-  float acc[kBlk];
-#pragma unroll
-  for (int c = 0; c < kBlk; c++) acc[c] = 0.f;
-  const int ctr = (warp + kCR) * SC_PW + (lane + kCR);
-#pragma unroll 1
-  for (int k = 0; k < kCN; k++) {
-    const int dy = k / kCW - kCR, dx = k % kCW - kCR;
-    const float cf = a.a_up[(long long)k * a.lvec + q];
-    const int sidx = ctr + dy * SC_PW + dx;
-#pragma unroll
-    for (int c = 0; c < kBlk; c++) acc[c] = fmaf(cf, yt[c * SC_PLANE + sidx], acc[c]);
-  }
-  float4* oq = (float4*)(out + q * kBlk);
-  const float4* xq = (const float4*)(X + q * kBlk);
-#pragma unroll
-  for (int c4 = 0; c4 < kBlk / 4; c4++) {
-    float4 r;
-    r.x = co.x * acc[4 * c4 + 0] + co.y * yt[(4 * c4 + 0) * SC_PLANE + ctr];
-    r.y = co.x * acc[4 * c4 + 1] + co.y * yt[(4 * c4 + 1) * SC_PLANE + ctr];
-    r.z = co.x * acc[4 * c4 + 2] + co.y * yt[(4 * c4 + 2) * SC_PLANE + ctr];
-    r.w = co.x * acc[4 * c4 + 3] + co.y * yt[(4 * c4 + 3) * SC_PLANE + ctr];
-    if (co.z != 0.f) {
-      const float4 xv = xq[c4];
-      r.x = fmaf(co.z, xv.x, r.x);
-      r.y = fmaf(co.z, xv.y, r.y);
-      r.z = fmaf(co.z, xv.z, r.z);
-      r.w = fmaf(co.z, xv.w, r.w);
-    }
-    oq[c4] = r;
+    c.wc[P * NC + k] = v;
   }
 }
 
@@ -497,18 +557,21 @@ cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const 
                            int step, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(cf_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStepSmem);
+    cudaFuncSetAttribute(cf_step_t<DiskStencil>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)StepSmem<DiskStencil>::bytes);
+    cudaFuncSetAttribute(cf_step_t<SquareStencil>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)StepSmem<SquareStencil>::bytes);
     attr = true;
   }
-  static bool attr_c = false;
-  if (!attr_c) {
-    cudaFuncSetAttribute(cf_step_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStepCSmem);
-    attr_c = true;
-  }
   if (a.coarse)
-    cf_step_c<<<nwork, ST_H * 32, kStepCSmem, s>>>(a, work, Y, X, out, step);
+    cf_step_t<SquareStencil><<<nwork, 256, StepSmem<SquareStencil>::bytes, s>>>(a, work, Y, X, out, step);
   else
-    cf_step<<<nwork, ST_H * 32, kStepSmem, s>>>(a, work, Y, X, out, step);
+    cf_step_t<DiskStencil><<<nwork, 256, StepSmem<DiskStencil>::bytes, s>>>(a, work, Y, X, out, step);
+  return cudaGetLastError();
+}
+cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwork, const float* a_up,
+                           const float* a_diag, long long lvec, float* afull, cudaStream_t s) {
+  cf_full<<<nwork, 256, 0, s>>>(patches, work16, a_up, a_diag, lvec, afull);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,

@@ -28,8 +28,9 @@ struct BlkArgs {
   const int* done;      // [npatch]
   const double* mat;    // [npatch][32*32]
   const double* theta;  // [npatch][32]
-  int coarse;           // 0: fine symmetric radius-5 stencil (a_up upper + a_diag)
-                        // 1: coarse full 7x7 stencil in a_up (kCN offsets)
+  int coarse;           // 0: fine radius-5 disk, 1: coarse 7 x 7 square
+  const float* afull;   // pixel-major stencil rows: 84 floats (fine) / 52 (coarse)
+  int* err;             // set to 1 when a tile's staging wait gave up
 };
 
 // coarse level (2 x 2 aggregation)
@@ -42,15 +43,18 @@ struct CoarseArgs {
   const float* wsym_up;  // fine symmetric affinities (upper offsets)
   const float* deg;      // fine degrees
   long long lvec_f, lvec_c;
-  float* wc;             // [kCN][lvec_c]: W_c, then A_c
+  float* wc;             // [lvec_c][kCoarseNC] pixel-major: W_c, then A_c
   float* degc;
   float* disc;
 };
 cudaError_t cf_launch_coarsen(const CoarseArgs& c, int nwork_c, cudaStream_t s);
+cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwork, const float* a_up,
+                           const float* a_diag, long long lvec, float* afull, cudaStream_t s);
 cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc, float* xf, cudaStream_t s);
 
 void upload_block(const HostTables& t, cudaStream_t s);
-constexpr int kStepTileH = 8, kStepTileW = 32;  // cf_step tile (work list entries)
+constexpr int kStepTileH = 8, kStepTileW = 16;  // cf_step tile (work list entries)
+constexpr int kFullNC = 84, kCoarseNC = 52;      // floats per pixel-major stencil row
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
                            int step, cudaStream_t s);
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
