@@ -20,6 +20,8 @@
 // project's own.
 #include <stdint.h>
 #include <stdio.h>
+
+#include <algorithm>
 #include <stdlib.h>
 
 #include "gpb_internal.h"
@@ -60,8 +62,6 @@ void upload_block(const HostTables& t, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_bup_dy, dy, sizeof(dy), 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_bup_dx, dx, sizeof(dx), 0, cudaMemcpyHostToDevice, s);
 }
-
-constexpr unsigned FULLB = 0xffffffffu;
 
 __device__ __forceinline__ void fma4(float4& acc, float a, const float4& x) {
   acc.x = fmaf(a, x.x, acc.x);
@@ -115,7 +115,18 @@ struct StepSmem {
   static constexpr int PH = ST_TY + 2 * S::R, PW = ST_TX + 2 * S::R;
   static constexpr size_t y_bytes = (size_t)PH * PW * kBlk * sizeof(float);
   static constexpr size_t c_bytes = (size_t)ST_TY * ST_TX * S::NC * sizeof(float);
-  static constexpr size_t bytes = y_bytes + c_bytes + 16;  // + the mbarrier
+  static constexpr size_t stage = y_bytes + c_bytes;  // one pipeline stage
+  static constexpr size_t bytes = 2 * stage + 256;    // two stages, tile records, mbarriers
+  static_assert(stage % 128 == 0, "stage alignment");
+};
+
+// what the producer warp tells the consumers about the tile in a stage
+struct StepMeta {
+  int end;        // 1: no more tiles for this CTA
+  int W, H, y0;
+  long long vec;
+  int x0, pad;
+  float cx, cy, cz, pad2;
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -125,6 +136,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
@@ -145,6 +159,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 // polls of the tile's barrier before a CTA gives up (each poll may suspend
 // the thread for a short hardware-defined time; the copies take microseconds)
 constexpr int kBarSpin = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int it = 0; it < kBarSpin; it++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
 
 template <int K>
 __device__ __forceinline__ float f4get(const float4& v) {
@@ -192,61 +211,120 @@ __device__ __forceinline__ void step_positions(const float* __restrict__ ys, con
   }
 }
 
+// Persistent, warp-specialised: one CTA per SM walks its share of the tile
+// list.  Warp 8 (one lane) is the producer: for each active tile it waits
+// until the consumers have released the stage, writes the tile record and
+// issues the bulk copies against the stage's "full" mbarrier.  Warps 0-7
+// consume: wait "full", prefetch X, run the stencil on their 4 x 4 block,
+// write the outputs and arrive on the stage's "empty" mbarrier.  Two stages,
+// so tile i+1 streams in while tile i is computed.  Every wait is bounded;
+// a wait that gives up sets *a.err and ends the CTA.
+constexpr int kStepConsumers = 8, kStepThreads = (kStepConsumers + 1) * 32;
+
 template <class S>
-__global__ void __launch_bounds__(256, 2) cf_step_t(BlkArgs a, const int4* __restrict__ work,
-                                                    const float* __restrict__ Y, const float* __restrict__ X,
-                                                    float* __restrict__ out, int step) {
+__global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const int4* __restrict__ work, int nwork,
+                                                             const float* __restrict__ Y, const float* __restrict__ X,
+                                                             float* __restrict__ out, int step) {
   using SM = StepSmem<S>;
   extern __shared__ __align__(128) unsigned char smem[];
-  float* ys = (float*)smem;                     // [PH][PW][32]
-  float* cs = (float*)(smem + SM::y_bytes);     // [TY * TX][NC]
-  uint64_t* bar = (uint64_t*)(smem + SM::y_bytes + SM::c_bytes);
-  const int4 w = work[blockIdx.x];              // (patch, y0, x0, -)
-  if (!a.active[w.x]) return;
-  const PatchDev P = a.patches[w.x];
-  const int ylast = min(w.y + ST_TY - 1, P.H - 1);  // rows past it feed no in-patch pixel
-  if (threadIdx.x == 0) mbar_init(bar, 1);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int ny = ylast - w.y + 1 + 2 * S::R, nc = ylast - w.y + 1;
-    constexpr uint32_t yrow = SM::PW * kBlk * sizeof(float), crow = ST_TX * S::NC * sizeof(float);
-    mbar_expect_tx(bar, (uint32_t)ny * yrow + (uint32_t)nc * crow);
-    for (int r = 0; r < ny; r++)
-      bulk_g2s(ys + (size_t)r * SM::PW * kBlk,
-               Y + (P.vec + (long long)(w.y - S::R + r) * P.W + (w.z - S::R)) * kBlk, yrow, bar);
-    for (int r = 0; r < nc; r++)
-      bulk_g2s(cs + (size_t)r * ST_TX * S::NC, a.afull + (P.vec + (long long)(w.y + r) * P.W + w.z) * S::NC, crow,
-               bar);
-  }
-  bool ready = false;
-  for (int it = 0; it < kBarSpin; it++)
-    if (mbar_try_wait(bar, 0)) {
-      ready = true;
-      break;
-    }
-  if (!ready) {  // record it, let the copies land, leave the tile undone
-    if (threadIdx.x == 0) atomicExch(a.err, 1);
-    for (int it = 0; it < kBarSpin && !mbar_try_wait(bar, 0); it++) {
-    }
-    return;
-  }
+  StepMeta* meta = (StepMeta*)(smem + 2 * SM::stage);  // [2]
+  uint64_t* full = (uint64_t*)(smem + 2 * SM::stage + 128);
+  uint64_t* empty = full + 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    mbar_init(full + 0, 1);
+    mbar_init(full + 1, 1);
+    mbar_init(empty + 0, kStepConsumers);
+    mbar_init(empty + 1, kStepConsumers);
+  }
+  __syncthreads();
+  if (warp == kStepConsumers) {  // ------------------------------- producer
+    if (lane != 0) return;
+    int i = 0;
+    for (int t = blockIdx.x;; t += gridDim.x, i++) {
+      int4 w = make_int4(0, 0, 0, 0);
+      bool have = false;
+      for (; t < nwork; t += gridDim.x) {
+        w = work[t];
+        if (a.active[w.x]) {
+          have = true;
+          break;
+        }
+      }
+      const int st = i & 1;
+      if (i >= 2 && !mbar_wait(empty + st, ((i >> 1) - 1) & 1)) {
+        atomicExch(a.err, 1);
+        return;
+      }
+      StepMeta& m = meta[st];
+      if (!have) {
+        m.end = 1;
+        mbar_arrive(full + st);
+        return;
+      }
+      const PatchDev P = a.patches[w.x];
+      const float3 co = a.coef[(long long)w.x * a.max_steps + step];
+      m.end = 0;
+      m.W = P.W;
+      m.H = P.H;
+      m.y0 = w.y;
+      m.x0 = w.z;
+      m.vec = P.vec;
+      m.cx = co.x;
+      m.cy = co.y;
+      m.cz = co.z;
+      // rows past the patch's last row (+ the radius) feed no in-patch pixel
+      const int ylast = min(w.y + ST_TY - 1, P.H - 1);
+      const int ny = ylast - w.y + 1 + 2 * S::R, nc = ylast - w.y + 1;
+      constexpr uint32_t yrow = SM::PW * kBlk * sizeof(float), crow = ST_TX * S::NC * sizeof(float);
+      float* ys = (float*)(smem + st * SM::stage);
+      float* cs = (float*)(smem + st * SM::stage + SM::y_bytes);
+      mbar_expect_tx(full + st, (uint32_t)ny * yrow + (uint32_t)nc * crow);
+      for (int r = 0; r < ny; r++)
+        bulk_g2s(ys + (size_t)r * SM::PW * kBlk,
+                 Y + (P.vec + (long long)(w.y - S::R + r) * P.W + (w.z - S::R)) * kBlk, yrow, full + st);
+      for (int r = 0; r < nc; r++)
+        bulk_g2s(cs + (size_t)r * ST_TX * S::NC, a.afull + (P.vec + (long long)(w.y + r) * P.W + w.z) * S::NC,
+                 crow, full + st);
+    }
+  }
+  // ------------------------------------------------------------ consumers
   const int by = (warp / (ST_TX / ST_B)) * ST_B, bx = (warp % (ST_TX / ST_B)) * ST_B;
-  float acc[16];
-  float4 cw[16];
+  for (int i = 0;; i++) {
+    const int st = i & 1;
+    if (!mbar_wait(full + st, (i >> 1) & 1)) {
+      if (lane == 0) atomicExch(a.err, 1);
+      return;
+    }
+    const StepMeta m = meta[st];
+    if (m.end) return;
+    const float* ys = (const float*)(smem + st * SM::stage);
+    const float* cs = (const float*)(smem + st * SM::stage + SM::y_bytes);
+    // the previous iterate's values for this lane's column, fetched now so
+    // the loads overlap the stencil
+    float xr[16];
 #pragma unroll
-  for (int i = 0; i < 16; i++) acc[i] = 0.f;
-  step_positions<S, 0>(ys + (by * SM::PW + bx) * kBlk + lane, cs + (by * ST_TX + bx) * S::NC, cw, acc);
-  const float3 co = a.coef[(long long)w.x * a.max_steps + step];
+    for (int k = 0; k < 16; k++) {
+      const int y = m.y0 + by + k / ST_B, x = m.x0 + bx + k % ST_B;
+      xr[k] = (m.cz != 0.f && y < m.H && x < m.W) ? X[(m.vec + (long long)y * m.W + x) * kBlk + lane] : 0.f;
+    }
+    float acc[16];
+    float4 cw[16];
 #pragma unroll
-  for (int i = 0; i < 16; i++) {
-    const int y = w.y + by + i / ST_B, x = w.z + bx + i % ST_B;
-    if (y >= P.H || x >= P.W) continue;
-    const long long q = P.vec + (long long)y * P.W + x;
-    const float yc = ys[((by + i / ST_B + S::R) * SM::PW + bx + i % ST_B + S::R) * kBlk + lane];
-    float r = co.x * acc[i] + co.y * yc;
-    if (co.z != 0.f) r = fmaf(co.z, X[q * kBlk + lane], r);
-    out[q * kBlk + lane] = r;
+    for (int k = 0; k < 16; k++) acc[k] = 0.f;
+    step_positions<S, 0>(ys + (by * SM::PW + bx) * kBlk + lane, cs + (by * ST_TX + bx) * S::NC, cw, acc);
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      const int y = m.y0 + by + k / ST_B, x = m.x0 + bx + k % ST_B;
+      if (y >= m.H || x >= m.W) continue;
+      const long long q = m.vec + (long long)y * m.W + x;
+      const float yc = ys[((by + k / ST_B + S::R) * SM::PW + bx + k % ST_B + S::R) * kBlk + lane];
+      float r = m.cx * acc[k] + m.cy * yc;
+      if (m.cz != 0.f) r = fmaf(m.cz, xr[k], r);
+      out[q * kBlk + lane] = r;
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(empty + st);
   }
 }
 
@@ -555,18 +633,24 @@ cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc,
 
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
                            int step, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncSetAttribute(cf_step_t<DiskStencil>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)StepSmem<DiskStencil>::bytes);
     cudaFuncSetAttribute(cf_step_t<SquareStencil>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)StepSmem<SquareStencil>::bytes);
-    attr = true;
+    if (nsm <= 0) nsm = 1;
   }
+  const int grid = std::min(nwork, nsm);  // one persistent CTA per SM
+  if (grid <= 0) return cudaSuccess;
   if (a.coarse)
-    cf_step_t<SquareStencil><<<nwork, 256, StepSmem<SquareStencil>::bytes, s>>>(a, work, Y, X, out, step);
+    cf_step_t<SquareStencil><<<grid, kStepThreads, StepSmem<SquareStencil>::bytes, s>>>(a, work, nwork, Y, X, out,
+                                                                                      step);
   else
-    cf_step_t<DiskStencil><<<nwork, 256, StepSmem<DiskStencil>::bytes, s>>>(a, work, Y, X, out, step);
+    cf_step_t<DiskStencil><<<grid, kStepThreads, StepSmem<DiskStencil>::bytes, s>>>(a, work, nwork, Y, X, out, step);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwork, const float* a_up,
