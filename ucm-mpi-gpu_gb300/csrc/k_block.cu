@@ -9,8 +9,8 @@
 //   cf_step    Y' = alpha (A Y) + beta Y + gamma X   (scaled Chebyshev
 //              recurrence, Zhou & Saad 2007; with alpha=1, beta=gamma=0 it
 //              is the plain block SpMV)
-//   cf_gram    G = U^T V per patch (32 x 32), compensated FP32 products,
-//              FP64 cross-CTA sums by the last CTA of the patch
+//   cf_gram    G = U^T V per patch (32 x 32), FP32 FMA runs folded into
+//              float-float sums, FP64 cross-CTA sums by the last CTA
 //   cf_rotate  U <- U M (32 x 32 per patch), optionally V <- V M too
 //   cf_resid   |A x_c - theta_c x_c|^2 per column
 //   cf_extract the first nvec columns into separate vectors (sPb layout)
@@ -373,41 +373,74 @@ __device__ __forceinline__ void ffp(float& hi, float& lo, float a, float b) {
   hi = s;
 }
 
-// G = U^T V: thread owns entries (i, j) = (tid / 8, 4*(tid % 8) .. +3) of the
-// 32 x 32 product; rows of U and V staged through shared memory
+// G = U^T V over a tile of pixels.  Chunks of 256 pixel rows of U and V are
+// staged in shared memory; four groups of 64 threads take 64 rows each, a
+// thread owning a 4 x 4 block of G (two broadcast 16-byte loads feed 16
+// FMAs).  Each group's 64-term FP32 FMA runs are folded into a float-float
+// (hi, lo) pair by an error-free TwoSum, so the sum over the tile is as
+// accurate as a compensated one at about the cost of plain FMAs; the four
+// groups and then the tiles are summed in FP64.
+constexpr int GR_CH = 256;  // pixels per staged chunk
+__device__ __forceinline__ void two_sum_into(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+
 __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restrict__ U,
                                                const float* __restrict__ V, double* __restrict__ out) {
   const EigTile t = a.tiles[blockIdx.x];
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
-  constexpr int CH = 64;  // pixels per stage
-  __shared__ float us[CH][kBlk + 1], vs[CH][kBlk + 1];
-  const int i = threadIdx.x >> 3, j0 = (threadIdx.x & 7) * 4;
-  float hi[4] = {0, 0, 0, 0}, lo[4] = {0, 0, 0, 0};
-  for (int p0 = t.p0; p0 < t.p1; p0 += CH) {
+  extern __shared__ __align__(16) float gsm[];  // us[GR_CH][32], vs[GR_CH][32]; reused for the group sums
+  float* us = gsm;
+  float* vs = gsm + GR_CH * kBlk;
+  const int grp = threadIdx.x >> 6, lt = threadIdx.x & 63;
+  const int i0 = (lt >> 3) * 4, j0 = (lt & 7) * 4;
+  float hi[16], lo[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) hi[k] = lo[k] = 0.f;
+  for (int p0 = t.p0; p0 < t.p1; p0 += GR_CH) {
     __syncthreads();
-    for (int idx = threadIdx.x; idx < CH * kBlk; idx += blockDim.x) {
-      const int pp = idx / kBlk, c = idx % kBlk;
+    for (int f = threadIdx.x; f < GR_CH * kBlk / 4; f += blockDim.x) {
+      const int pp = f / (kBlk / 4), c4 = f % (kBlk / 4);
       const int p = p0 + pp;
-      float u = 0.f, v = 0.f;
+      float4 u = make_float4(0.f, 0.f, 0.f, 0.f), v = u;
       if (p < t.p1) {
-        u = U[(P.vec + p) * kBlk + c];
-        v = V[(P.vec + p) * kBlk + c];
+        u = ((const float4*)(U + (P.vec + p) * kBlk))[c4];
+        v = ((const float4*)(V + (P.vec + p) * kBlk))[c4];
       }
-      us[pp][c] = u;
-      vs[pp][c] = v;
+      ((float4*)us)[f] = u;
+      ((float4*)vs)[f] = v;
     }
     __syncthreads();
+    float acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) acc[k] = 0.f;
+    const int pbeg = grp * (GR_CH / 4);
 #pragma unroll 4
-    for (int pp = 0; pp < CH; pp++) {
-      const float ui = us[pp][i];
+    for (int pp = pbeg; pp < pbeg + GR_CH / 4; pp++) {
+      const float4 u4 = *(const float4*)(us + pp * kBlk + i0);
+      const float4 v4 = *(const float4*)(vs + pp * kBlk + j0);
+      const float uu[4] = {u4.x, u4.y, u4.z, u4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
 #pragma unroll
-      for (int q = 0; q < 4; q++) ffp(hi[q], lo[q], ui, vs[pp][j0 + q]);
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[r * 4 + c] = fmaf(uu[r], vv[c], acc[r * 4 + c]);
     }
-  }
-  double* part = a.part + (long long)blockIdx.x * kBlk * kBlk;
 #pragma unroll
-  for (int q = 0; q < 4; q++) part[i * kBlk + j0 + q] = (double)hi[q] + (double)lo[q];
+    for (int k = 0; k < 16; k++) two_sum_into(hi[k], lo[k], acc[k]);
+  }
+  // the four groups' blocks, summed in FP64
+  __syncthreads();
+  double* red = (double*)gsm;  // [4][32 * 32]
+#pragma unroll
+  for (int k = 0; k < 16; k++) red[grp * kBlk * kBlk + (i0 + k / 4) * kBlk + j0 + k % 4] = (double)hi[k] + (double)lo[k];
+  __syncthreads();
+  double* part = a.part + (long long)blockIdx.x * kBlk * kBlk;
+  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x)
+    part[e] = red[e] + red[kBlk * kBlk + e] + red[2 * kBlk * kBlk + e] + red[3 * kBlk * kBlk + e];
   // last CTA of the patch sums the partials
   __shared__ int is_last;
   __syncthreads();
@@ -436,7 +469,7 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
   const EigTile t = a.tiles[blockIdx.x];
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
-  __shared__ float mh[kBlk][kBlk];
+  __shared__ __align__(16) float mh[kBlk][kBlk];
   const double* M = a.mat + (long long)t.patch * kBlk * kBlk;
   for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) mh[e / kBlk][e % kBlk] = (float)M[e];
   __syncthreads();
@@ -457,10 +490,11 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
         float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int r = 0; r < kBlk; r++) {
-          o.x = fmaf(x[r], mh[r][c0], o.x);
-          o.y = fmaf(x[r], mh[r][c0 + 1], o.y);
-          o.z = fmaf(x[r], mh[r][c0 + 2], o.z);
-          o.w = fmaf(x[r], mh[r][c0 + 3], o.w);
+          const float4 m4 = *(const float4*)&mh[r][c0];  // broadcast: every thread reads the same row
+          o.x = fmaf(x[r], m4.x, o.x);
+          o.y = fmaf(x[r], m4.y, o.y);
+          o.z = fmaf(x[r], m4.z, o.z);
+          o.w = fmaf(x[r], m4.w, o.w);
         }
         if (c0 < ncols) *(float4*)(row + c0) = o;
       }
@@ -660,7 +694,13 @@ cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwor
 }
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
                            cudaStream_t s) {
-  cf_gram<<<ntiles, 256, 0, s>>>(a, U, V, out);
+  constexpr int smem = 2 * GR_CH * kBlk * sizeof(float);  // 64 KB; the FP64 group sums (32 KB) reuse it
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(cf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  cf_gram<<<ntiles, 256, smem, s>>>(a, U, V, out);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s) {
