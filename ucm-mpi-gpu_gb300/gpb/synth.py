@@ -155,3 +155,24 @@ def grid_patches(H, W, rows, cols, halo):
             x0, x1 = max(0, b0 - halo), min(W, b1 + halo)
             out.append((y0, x0, y1 - y0, x1 - x0, a0 - y0, b0 - x0, a1 - a0, b1 - b0))
     return out
+
+
+def config3():
+    """4096 x 4096, 4096 cells, sigma 6, 40 lines: the uneven-batching image.
+    Returns (image, codebook, boxes) with 64 rectangles whose sides are uniform
+    in [200, 700] px at uniform positions, as (y0, x0, h, w)."""
+    img = voronoi_image(4096, 4096, 4096, 6.0, SEED_BASE + 3, lines=40)
+    rng = np.random.default_rng(SEED_BASE + 33)
+    boxes = []
+    for _ in range(64):
+        h, w = (int(v) for v in rng.integers(200, 701, 2))
+        y0, x0 = int(rng.integers(0, 4096 - h + 1)), int(rng.integers(0, 4096 - w + 1))
+        boxes.append((y0, x0, h, w))
+    return img, make_codebook(img, SEED_BASE + 3), boxes
+
+
+def config5():
+    """8192 x 8192, 16384 cells, sigma 8, 200 lines: 256 patches of 512^2 with
+    a 5-px halo (grid_patches(8192, 8192, 16, 16, 5))."""
+    img = voronoi_image(8192, 8192, 16384, 8.0, SEED_BASE + 5, lines=200)
+    return img, make_codebook(img, SEED_BASE + 5)
