@@ -323,7 +323,7 @@ extern "C" void gpb_default_params(gpb_params* p) {
   p->eig_mode = GPB_EIG_LANCZOS;
   p->keep_intermediates = 0;
   p->cheb_degree = 40;
-  p->warm_tol = 1e-3f;
+  p->warm_tol = 3e-3f;
 }
 
 extern "C" const char* gpb_status_str(gpb_status s) {

@@ -22,8 +22,7 @@ namespace gpb {
 
 __constant__ float c_k32[kNschmid][kSchmidGroups];
 __constant__ int c_goff_start[kSchmidGroups + 1];
-__constant__ int8_t c_goff_dy[2401];
-__constant__ int8_t c_goff_dx[2401];
+__constant__ int16_t c_goff_off[2401];  // dy * 64 + dx: the displacement in the 64-wide staged tile
 __constant__ float c_codebook[kNschmid][kMaxCodewords];
 __constant__ float c_errb[kNschmid];
 __constant__ double c_gamma[256];
@@ -50,8 +49,9 @@ void upload_front(const HostTables& t, cudaStream_t s) {
   }
   start[kSchmidGroups] = n;
   cudaMemcpyToSymbolAsync(c_goff_start, start, sizeof(start), 0, cudaMemcpyHostToDevice, s);
-  cudaMemcpyToSymbolAsync(c_goff_dy, dy, sizeof(dy), 0, cudaMemcpyHostToDevice, s);
-  cudaMemcpyToSymbolAsync(c_goff_dx, dx, sizeof(dx), 0, cudaMemcpyHostToDevice, s);
+  int16_t off[2401];
+  for (int j = 0; j < n; j++) off[j] = (int16_t)(dy[j] * 64 + dx[j]);
+  cudaMemcpyToSymbolAsync(c_goff_off, off, sizeof(int16_t) * n, 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_errb, t.err_bound, sizeof(t.err_bound), 0, cudaMemcpyHostToDevice, s);
   cudaMemcpyToSymbolAsync(c_gamma, t.gamma_lut, sizeof(t.gamma_lut), 0, cudaMemcpyHostToDevice, s);
 }
@@ -112,11 +112,18 @@ __global__ void __launch_bounds__(256) k_convert(const uint32_t* __restrict__ pa
 // ----------------------------------------------------------------- texton
 constexpr int TX_T = 16;              // 16 x 16 outputs per block
 constexpr int TX_W = TX_T + 2 * 24;   // 64
+static_assert(TX_W == 64, "c_goff_off is built for a 64-wide staged tile");
 
-__global__ void __launch_bounds__(256) k_texton(const PatchDev* __restrict__ patches,
-                                                const int4* __restrict__ work, const uint8_t* __restrict__ grey,
-                                                uint32_t* __restrict__ lab4, int* __restrict__ repair_list,
-                                                int* __restrict__ repair_count, int repair_cap) {
+// 64 threads per 16 x 16 tile: a thread owns the 4 pixels (ty0 + 4k, tx),
+// so every offset-table and filter-weight load from constant memory serves
+// four pixels (the kernel is bound by those loads, not by arithmetic)
+constexpr int TX_THREADS = 64, TX_PIX = TX_T * TX_T / TX_THREADS;  // 4 pixels per thread
+
+__global__ void __launch_bounds__(TX_THREADS) k_texton(const PatchDev* __restrict__ patches,
+                                                       const int4* __restrict__ work,
+                                                       const uint8_t* __restrict__ grey,
+                                                       uint32_t* __restrict__ lab4, int* __restrict__ repair_list,
+                                                       int* __restrict__ repair_count, int repair_cap) {
   __shared__ uint8_t tile[TX_W * TX_W];
   const int4 w = work[blockIdx.x];  // (patch, ty0, tx0, -)
   const PatchDev P = patches[w.x];
@@ -126,65 +133,78 @@ __global__ void __launch_bounds__(256) k_texton(const PatchDev* __restrict__ pat
     tile[i] = g[(long long)yy * P.W + xx];
   }
   __syncthreads();
-  const int ty = threadIdx.x / TX_T, tx = threadIdx.x % TX_T;
-  const int y = w.y + ty, x = w.z + tx;
-  if (y >= P.H || x >= P.W) return;
+  const int ty0 = threadIdx.x / TX_T, tx = threadIdx.x % TX_T;
+  constexpr int ROWSTEP = TX_THREADS / TX_T;  // 4
   // FMA accumulation: |error of R_f| <= u * sum_k |partial sum_k| (each step
   // rounds once), tracked at run time in E_f
-  float R[kNschmid], E[kNschmid];
+  float R[TX_PIX][kNschmid], E[TX_PIX][kNschmid];
 #pragma unroll
-  for (int f = 0; f < kNschmid; f++) R[f] = E[f] = 0.f;
-  const uint8_t* c = tile + (ty + 24) * TX_W + (tx + 24);
+  for (int k = 0; k < TX_PIX; k++)
+#pragma unroll
+    for (int f = 0; f < kNschmid; f++) R[k][f] = E[k][f] = 0.f;
+  const uint8_t* c = tile + (ty0 + 24) * TX_W + (tx + 24);
   for (int gi = 0; gi < kSchmidGroups; gi++) {
-    int s = 0;
+    int sum[TX_PIX] = {0, 0, 0, 0};
     const int e = c_goff_start[gi + 1];
-    for (int j = c_goff_start[gi]; j < e; j++) s += c[c_goff_dy[j] * TX_W + c_goff_dx[j]];
-    const float sf = (float)s;
+    for (int j = c_goff_start[gi]; j < e; j++) {
+      const int off = c_goff_off[j];
+#pragma unroll
+      for (int k = 0; k < TX_PIX; k++) sum[k] += c[off + k * ROWSTEP * TX_W];
+    }
 #pragma unroll
     for (int f = 0; f < kNschmid; f++) {
-      R[f] = fmaf(c_k32[f][gi], sf, R[f]);
-      E[f] += fabsf(R[f]);
+      const float kf = c_k32[f][gi];
+#pragma unroll
+      for (int k = 0; k < TX_PIX; k++) {
+        R[k][f] = fmaf(kf, (float)sum[k], R[k][f]);
+        E[k][f] += fabsf(R[k][f]);
+      }
     }
   }
-#pragma unroll
-  for (int f = 0; f < kNschmid; f++) E[f] = E[f] * 6.0e-8f * 1.01f + 1e-6f;
   const int K = c_K;
-  float d1 = 3.4e38f, d2 = 3.4e38f;
-  int k1 = 0, k2 = 0;
-  for (int k = 0; k < K; k++) {
-    float d = 0.f;
+#pragma unroll
+  for (int k = 0; k < TX_PIX; k++) {
+    const int y = w.y + ty0 + k * ROWSTEP, x = w.z + tx;
+    if (y >= P.H || x >= P.W) continue;
+#pragma unroll
+    for (int f = 0; f < kNschmid; f++) E[k][f] = E[k][f] * 6.0e-8f * 1.01f + 1e-6f;
+    float d1 = 3.4e38f, d2 = 3.4e38f;
+    int k1 = 0, k2 = 0;
+    for (int q = 0; q < K; q++) {
+      float d = 0.f;
+#pragma unroll
+      for (int f = 0; f < kNschmid; f++) {
+        const float t = R[k][f] - c_codebook[f][q];
+        d = fmaf(t, t, d);
+      }
+      if (d < d1) {
+        d2 = d1;
+        k2 = k1;
+        d1 = d;
+        k1 = q;
+      } else if (d < d2) {
+        d2 = d;
+        k2 = q;
+      }
+    }
+    // error bound of d(k1) and d(k2): responses off by at most E_f each, plus
+    // the FP32 rounding of the distance sums themselves
+    float margin = 0.f;
 #pragma unroll
     for (int f = 0; f < kNschmid; f++) {
-      const float t = R[f] - c_codebook[f][k];
-      d = fmaf(t, t, d);
+      const float eb = E[k][f];
+      margin += 2.f * eb * (fabsf(R[k][f] - c_codebook[f][k1]) + fabsf(R[k][f] - c_codebook[f][k2]) + eb);
     }
-    if (d < d1) {
-      d2 = d1;
-      k2 = k1;
-      d1 = d;
-      k1 = k;
-    } else if (d < d2) {
-      d2 = d;
-      k2 = k;
-    }
-  }
-  // error bound of d(k1) and d(k2): responses off by at most E_f each, plus
-  // the FP32 rounding of the distance sums themselves
-  float margin = 0.f;
-#pragma unroll
-  for (int f = 0; f < kNschmid; f++) {
-    const float e = E[f];
-    margin += 2.f * e * (fabsf(R[f] - c_codebook[f][k1]) + fabsf(R[f] - c_codebook[f][k2]) + e);
-  }
-  margin = 2.f * margin + 4e-6f * (d1 + d2) + 1e-6f;
-  const long long pix = P.pix + (long long)y * P.W + x;
-  uint32_t v = lab4[pix] & 0x00ffffffu;
-  lab4[pix] = v | ((uint32_t)k1 << 24);
-  if (K > 1 && d2 - d1 <= margin) {
-    const int slot = atomicAdd(repair_count, 1);
-    if (slot < repair_cap) {
-      repair_list[2 * slot] = w.x;
-      repair_list[2 * slot + 1] = y * P.W + x;
+    margin = 2.f * margin + 4e-6f * (d1 + d2) + 1e-6f;
+    const long long pix = P.pix + (long long)y * P.W + x;
+    uint32_t v = lab4[pix] & 0x00ffffffu;
+    lab4[pix] = v | ((uint32_t)k1 << 24);
+    if (K > 1 && d2 - d1 <= margin) {
+      const int slot = atomicAdd(repair_count, 1);
+      if (slot < repair_cap) {
+        repair_list[2 * slot] = w.x;
+        repair_list[2 * slot + 1] = y * P.W + x;
+      }
     }
   }
 }
@@ -262,7 +282,7 @@ cudaError_t launch_texton(const PatchDev* patches, const int4* work, int nwork, 
                           uint32_t* lab4, int* repair_list, int* repair_count, int repair_cap,
                           cudaStream_t s) {
   if (nwork == 0) return cudaSuccess;
-  k_texton<<<nwork, 256, 0, s>>>(patches, work, grey, lab4, repair_list, repair_count, repair_cap);
+  k_texton<<<nwork, TX_THREADS, 0, s>>>(patches, work, grey, lab4, repair_list, repair_count, repair_cap);
   return cudaGetLastError();
 }
 
