@@ -305,3 +305,29 @@ def test_config2_batch_properties(orc):
         X = ctx.fetch("evecs", i, (9, h * w), np.float32).astype(np.float64)
         assert _residuals(orc, Wg, ev, X).max() <= 1e-4
     ctx.close()
+
+
+def test_config3_uneven_batch(orc):
+    """64 rectangles with sides in [200, 700] of a 4096^2 image (4096 cells,
+    sigma 6, 40 lines), one warm-started batch: every patch converges, the
+    outputs are finite gPb maps, and the two smallest patches match their own
+    oracle runs within the gPb tolerance."""
+    import gpb
+    from gpb import synth
+    img, cb, boxes = synth.config3()
+    crops = [np.ascontiguousarray(img[y0:y0 + h, x0:x0 + w]) for (y0, x0, h, w) in boxes]
+    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
+    outs = ctx.compute_batch([synth.pack_bgr(c) for c in crops])
+    assert ctx.last_status == gpb.GPB_OK
+    st = ctx.stats()
+    assert 0 < st["max_residual"] <= 3 * ctx.params.eig_tol
+    for (nm, orr), (_, _, h, w) in zip(outs, boxes):
+        assert nm.shape == (h, w) and orr.size == 8 * h * w
+        assert np.isfinite(nm).all() and np.isfinite(orr).all() and nm.min() >= 0
+    smallest = sorted(range(len(boxes)), key=lambda i: boxes[i][2] * boxes[i][3])[:2]
+    for i in smallest:
+        ref = orc.globalpb(crops[i], cb)
+        h, w = boxes[i][2], boxes[i][3]
+        assert np.abs(outs[i][0] - ref["nmax"]).max() < GPB_TOL
+        assert np.abs(outs[i][1].reshape(8, h, w) - ref["gpb_o"]).max() < GPB_TOL
+    ctx.close()

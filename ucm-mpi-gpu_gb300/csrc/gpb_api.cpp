@@ -127,6 +127,7 @@ struct Buf {
   float* cdis = nullptr; size_t c_cdis = 0;
   float* cblk[4] = {nullptr, nullptr, nullptr, nullptr}; size_t c_cblk[4] = {0, 0, 0, 0};
   float* afull = nullptr; size_t c_afull = 0;  // pixel-major fine stencil rows
+  int4* work_act = nullptr; size_t c_wact = 0;  // block-step tiles of the still active patches
   int* berr = nullptr; size_t c_berr = 0;
 };
 
@@ -317,7 +318,7 @@ extern "C" void gpb_default_params(gpb_params* p) {
   p->compat = GPB_COMPAT_CPU;
   p->nvec = 9;
   p->eig_tol = 1e-6f;
-  p->eig_max_matvecs = 20000;
+  p->eig_max_matvecs = 100000;
   p->krylov_dim = 40;
   p->krylov_keep = 26;
   p->eig_mode = GPB_EIG_LANCZOS;
@@ -442,7 +443,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
                   b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
                   b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
                   b.bcoef, b.bdone, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk,
-                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr};
+                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr, b.work_act};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
@@ -632,6 +633,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
   if (q.eig_mode != GPB_EIG_LANCZOS) {
     for (int i = 0; i < 4; i++) es.push_back(grow(b.blk[i], b.c_blk[i], (size_t)kBlk * V));
     es.push_back(grow(b.afull, b.c_afull, (size_t)kFullNC * V));
+    es.push_back(grow(b.work_act, b.c_wact, L.work_blk.size()));
     es.push_back(grow(b.berr, b.c_berr, 1));
     es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
@@ -890,8 +892,15 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   const gpb_params& q = ctx->prm;
   cudaStream_t s = ctx->st;
   const int np = (int)L.patches.size(), nt = (int)L.tiles.size(), nev = q.nvec;
-  const int nwb = (int)L.work_blk.size();
+  // the persistent block step walks a tile list; once patches converge it
+  // gets only the tiles of the active ones (L.work_blk is patch-major)
+  std::vector<int> tb_begin(np + 1, 0);
+  for (const int4& t : L.work_blk) tb_begin[t.x + 1]++;
+  for (int i = 0; i < np; i++) tb_begin[i + 1] += tb_begin[i];
+  int nwb = (int)L.work_blk.size();
   const int4* work_blk = lv.work_blk;
+  std::vector<int4> act_tiles;
+  std::vector<int> listed(np, 1);  // the patches the current list holds
   // a multiple of 3, so the three-buffer Chebyshev rotation ends where it
   // started and every patch's vectors stay in X, converged or not
   const int deg = std::min((std::max(3, q.cheb_degree) + 2) / 3 * 3, kMaxCheb / 3 * 3);
@@ -1028,6 +1037,15 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     }
     CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     if (nactive == 0) break;
+    if (active != listed) {
+      act_tiles.clear();
+      for (int i = 0; i < np; i++)
+        if (active[i]) act_tiles.insert(act_tiles.end(), L.work_blk.begin() + tb_begin[i], L.work_blk.begin() + tb_begin[i + 1]);
+      CK(cudaMemcpyAsync(b.work_act, act_tiles.data(), act_tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, s));
+      work_blk = b.work_act;
+      nwb = (int)act_tiles.size();
+      listed = active;
+    }
     CK(cudaMemcpyAsync(b.bcoef, coef.data(), coef.size() * sizeof(float3), cudaMemcpyHostToDevice, s));
     // filter: buffers rotate X -> Y -> Z -> X ...
     long long apx = 0;

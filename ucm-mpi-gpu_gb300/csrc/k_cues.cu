@@ -75,9 +75,11 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int CT_H = kCueTileH, CT_W = kCueTileW;
 constexpr int CT_PH = CT_H + 2 * kMaxRadius, CT_PW = CT_W + 2 * kMaxRadius;
 constexpr int HROW = 36;                    // bytes per counter row
+constexpr int DROW = 12;                    // floats per bin row of the convolution scratch
 constexpr int HWARP = 4 * 32 * HROW;        // bytes per warp
 constexpr int CT_WARPS = CT_H;              // one warp per tile row
-constexpr size_t kCueSmem = (size_t)CT_PH * CT_PW * 4 + kAnnMax * 2 + (size_t)CT_WARPS * HWARP;
+constexpr size_t kCueSmem =
+    (size_t)CT_PH * CT_PW * 4 + kAnnMax * 2 + (size_t)CT_WARPS * HWARP + (size_t)CT_WARPS * 32 * DROW * 4;
 
 // Sum of 16 per-lane values over the warp, for all 16 at once: each exchange
 // step halves the number of live values (8+4+2+1+1 shuffles), then the 16
@@ -116,40 +118,42 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-// truncated 'same' convolution along bins (conv_in_place_1D,
-// lib_image.cc:3084-3115): out[n] = sum_j in[n + K/2 - j] k[j] over the
-// in-range sources; kw holds this lane's kernel with out-of-range taps zeroed
+// this lane's taps of a K-tap bin smoothing (zero where the source bin
+// lane + K/2 - j lies outside [0, nb), or the lane itself does) and the
+// kernel mass that source bin `lane` keeps in range; per patch, so computed
+// once per warp
 template <int K>
-__device__ __forceinline__ float bin_conv(float v, int lane, const float (&kw)[K > 0 ? K : 1]) {
-  float r = 0.f;
+__device__ __forceinline__ float bin_taps(const float* kern, int lane, int nb, float (&kw)[K]) {
+  float m = 0.f;
 #pragma unroll
-  for (int j = 0; j < K; j++) r = fmaf(__shfl_sync(FULL, v, (lane + K / 2 - j) & 31), kw[j], r);
-  return r;
+  for (int j = 0; j < K; j++) {
+    const int src = lane + K / 2 - j;
+    kw[j] = (lane < nb && src >= 0 && src < nb) ? kern[j] : 0.f;
+    const int n = lane + j - K / 2;
+    if (n >= 0 && n < nb) m += kern[j];
+  }
+  return m;
 }
 
+// per-warp scratch (DROW floats per bin): the 8 orientation differences and
+// the total; 12 floats so that 16-byte loads of neighbouring bins are
+// conflict-free
+
 // one (cue, radius): counts of bin `lane` in the 16 slices -> 8 chi-squared
-// terms of this bin accumulated with the two weight sets
+// terms of this bin accumulated with the two weight sets.  The truncated
+// 'same' bin convolution (conv_in_place_1D, lib_image.cc:3084-3115) of all 8
+// orientation differences and of the total runs on the warp's scratch rows.
 template <int K>
 __device__ __forceinline__ void cue_combo(const uint8_t* hist, int c, int lane, int nb, int ann,
-                                          const float* kern, float wm, float wg, float (&accm)[8],
-                                          float (&accg)[8], float* raw, long long raw_stride) {
+                                          const float (&kw)[K > 0 ? K : 1], float m, float wm, float wg,
+                                          float (&accm)[8], float (&accg)[8], float* raw, long long raw_stride,
+                                          float* dsm) {
   float cs[16];
 #pragma unroll
   for (int q = 0; q < 16; q++)
     cs[q] = lane < nb ? (float)(hist[(c * 32 + q) * HROW + lane] + hist[(c * 32 + 16 + q) * HROW + lane]) : 0.f;
   float S[16];
-  float kw[K > 0 ? K : 1];
   if (K > 0) {
-    // this lane's taps (zero where the source bin is outside [0, nb), or the
-    // lane itself is) and the kernel mass that source bin `lane` keeps in range
-    float m = 0.f;
-#pragma unroll
-    for (int j = 0; j < K; j++) {
-      const int src = lane + K / 2 - j;
-      kw[j] = (lane < nb && src >= 0 && src < nb) ? kern[j] : 0.f;
-      const int n = lane + j - K / 2;
-      if (n >= 0 && n < nb) m += kern[j];
-    }
 #pragma unroll
     for (int q = 0; q < 16; q++) S[q] = cs[q] * m;
     warp_sum16(S, lane);
@@ -165,19 +169,49 @@ __device__ __forceinline__ void cue_combo(const uint8_t* hist, int c, int lane, 
     T += ch[q];
     D += q < 8 ? ch[q] : -ch[q];
   }
-  if (K > 0) T = bin_conv<K>(T, lane, kw);
+  float Dv[8];
+#pragma unroll
+  for (int o = 0; o < 8; o++) {
+    Dv[o] = D;
+    D += 2.f * (ch[o + 8] - ch[o]);
+  }
+  if (K > 0) {
+    float* row = dsm + lane * DROW;
+    *(float4*)(row + 0) = make_float4(Dv[0], Dv[1], Dv[2], Dv[3]);
+    *(float4*)(row + 4) = make_float4(Dv[4], Dv[5], Dv[6], Dv[7]);
+    row[8] = T;
+    __syncwarp();
+    float cd[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, ct = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+      const float* src = dsm + ((lane + K / 2 - j) & 31) * DROW;
+      const float4 d0 = *(const float4*)(src + 0), d1 = *(const float4*)(src + 4);
+      const float kj = kw[j];
+      cd[0] = fmaf(d0.x, kj, cd[0]);
+      cd[1] = fmaf(d0.y, kj, cd[1]);
+      cd[2] = fmaf(d0.z, kj, cd[2]);
+      cd[3] = fmaf(d0.w, kj, cd[3]);
+      cd[4] = fmaf(d1.x, kj, cd[4]);
+      cd[5] = fmaf(d1.y, kj, cd[5]);
+      cd[6] = fmaf(d1.z, kj, cd[6]);
+      cd[7] = fmaf(d1.w, kj, cd[7]);
+      ct = fmaf(src[8], kj, ct);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int o = 0; o < 8; o++) Dv[o] = cd[o];
+    T = ct;
+  }
   const float rT = (T != 0.f && lane < nb) ? __frcp_rn(T) : 0.f;
 #pragma unroll
   for (int o = 0; o < 8; o++) {
-    const float Do = K > 0 ? bin_conv<K>(D, lane, kw) : D;
-    const float term = Do * Do * rT;
+    const float term = Dv[o] * Dv[o] * rT;
     accm[o] = fmaf(wm, term, accm[o]);
     accg[o] = fmaf(wg, term, accg[o]);
     if (raw) {
       const float chi = 0.5f * warp_sum(term);
       if (lane == 0) raw[o * raw_stride] = chi;
     }
-    D += 2.f * (ch[o + 8] - ch[o]);
   }
 }
 
@@ -205,8 +239,14 @@ __global__ void __launch_bounds__(CT_WARPS * 32) k_cues(const PatchDev* __restri
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   uint8_t* hist = hist_all + warp * HWARP;
+  float* dsm = (float*)(hist_all + (size_t)CT_WARPS * HWARP) + warp * 32 * DROW;
   const int nbL = nbins[4 * w.x + 0] + 1, nbA = nbins[4 * w.x + 1] + 1, nbB = nbins[4 * w.x + 2] + 1,
             nbT = nbins[4 * w.x + 3] + 1;
+  float kwL[17], kwA[9], kwB[9];
+  const float mL = bin_taps<17>(c_kbg, lane, nbL, kwL);
+  const float mA = bin_taps<9>(c_kcg, lane, nbA, kwA);
+  const float mB = bin_taps<9>(c_kcg, lane, nbB, kwB);
+  const float kw0[1] = {0.f};
   const int y = w.y + warp;
   if (y >= P.H) return;
   uint8_t* r0 = hist + (0 * 32 + lane) * HROW;
@@ -259,18 +299,19 @@ __global__ void __launch_bounds__(CT_WARPS * 32) k_cues(const PatchDev* __restri
       // cue index wi = cue*3 + scale (bg1 bg2 bg3 cga1 .. tg3)
       if (kRaw) rawp = raw + P.pix * 96 + p;
       if (a == 0) {
-        cue_combo<17>(hist, 0, lane, nbL, a, c_kbg, c_wm[0], c_wg[0], accm, accg, kRaw ? rawp + 0 * 8 * rs : nullptr, rs);
+        cue_combo<17>(hist, 0, lane, nbL, a, kwL, mL, c_wm[0], c_wg[0], accm, accg,
+                      kRaw ? rawp + 0 * 8 * rs : nullptr, rs, dsm);
       } else {
         const int s = a - 1;  // scale of cga/cgb/tg
         if (a < 3)
-          cue_combo<17>(hist, 0, lane, nbL, a, c_kbg, c_wm[a], c_wg[a], accm, accg,
-                        kRaw ? rawp + (long long)a * 8 * rs : nullptr, rs);
-        cue_combo<9>(hist, 1, lane, nbA, a, c_kcg, c_wm[3 + s], c_wg[3 + s], accm, accg,
-                     kRaw ? rawp + (long long)(3 + s) * 8 * rs : nullptr, rs);
-        cue_combo<9>(hist, 2, lane, nbB, a, c_kcg, c_wm[6 + s], c_wg[6 + s], accm, accg,
-                     kRaw ? rawp + (long long)(6 + s) * 8 * rs : nullptr, rs);
-        cue_combo<0>(hist, 3, lane, nbT, a, nullptr, c_wm[9 + s], c_wg[9 + s], accm, accg,
-                     kRaw ? rawp + (long long)(9 + s) * 8 * rs : nullptr, rs);
+          cue_combo<17>(hist, 0, lane, nbL, a, kwL, mL, c_wm[a], c_wg[a], accm, accg,
+                        kRaw ? rawp + (long long)a * 8 * rs : nullptr, rs, dsm);
+        cue_combo<9>(hist, 1, lane, nbA, a, kwA, mA, c_wm[3 + s], c_wg[3 + s], accm, accg,
+                     kRaw ? rawp + (long long)(3 + s) * 8 * rs : nullptr, rs, dsm);
+        cue_combo<9>(hist, 2, lane, nbB, a, kwB, mB, c_wm[6 + s], c_wg[6 + s], accm, accg,
+                     kRaw ? rawp + (long long)(6 + s) * 8 * rs : nullptr, rs, dsm);
+        cue_combo<0>(hist, 3, lane, nbT, a, kw0, 0.f, c_wm[9 + s], c_wg[9 + s], accm, accg,
+                     kRaw ? rawp + (long long)(9 + s) * 8 * rs : nullptr, rs, dsm);
       }
       __syncwarp();
     }
