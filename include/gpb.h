@@ -152,6 +152,30 @@ gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst, size_t ds
 
 gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st);
 
+/* Stitching the patches of the last compute call into whole-image planes on
+ * the device; replaces Pieces2Gpb (src/utilities.cpp:180-213). */
+typedef enum {
+  GPB_STITCH_LAST = 0,      /* each patch's whole box, in patch order: later patches
+                               overwrite the overlaps (the reference's rule)         */
+  GPB_STITCH_INTERIOR = 1,  /* each patch writes only its interior box               */
+  GPB_STITCH_BLEND = 2      /* overlaps averaged with weights falling linearly over
+                               `ramp` pixels towards each patch edge inside the image */
+} gpb_stitch_mode;
+
+typedef struct {
+  int32_t x0, y0;           /* the patch's top-left corner in the image              */
+  int32_t ix, iy, iw, ih;   /* its interior box, in patch coordinates                */
+} gpb_place;
+
+/* n must be the patch count of the last gpb_compute* call on ctx, in the same
+ * order.  d_nmax (width*height floats) and d_orient (8*width*height, plane
+ * after plane) receive row-major image planes in the patch output's plane
+ * order; pixels no patch covers are left as they were.  Device pointers;
+ * synchronous on the context's stream.  BLEND uses a context buffer of
+ * 10*width*height floats. */
+gpb_status gpb_stitch_device(gpb_ctx* ctx, int mode, uint32_t width, uint32_t height, const gpb_place* places,
+                             size_t n, int ramp, float* d_nmax, float* d_orient);
+
 /* Texton and Lab-bin labels of one image already on the device, computed
  * without allocating memory, on the device or the host.  No counterpart in
  * the reference: its texton stage (src/SPFeatures.cpp:277-360) allocates

@@ -128,6 +128,7 @@ struct Buf {
   float* cblk[4] = {nullptr, nullptr, nullptr, nullptr}; size_t c_cblk[4] = {0, 0, 0, 0};
   float* afull = nullptr; size_t c_afull = 0;  // pixel-major fine stencil rows
   int4* work_act = nullptr; size_t c_wact = 0;  // block-step tiles of the still active patches
+  float* stitch = nullptr; size_t c_stitch = 0;  // BLEND accumulators [10][image]
   int* berr = nullptr; size_t c_berr = 0;
 };
 
@@ -443,7 +444,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
                   b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
                   b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
                   b.bcoef, b.bdone, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk,
-                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr, b.work_act};
+                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr, b.work_act, b.stitch};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
@@ -929,6 +930,13 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   std::vector<float3> coef(np * (size_t)kMaxCheb);
   std::vector<float> evals((size_t)np * nev, 0.f);
   std::vector<long> mv(np, 0);
+  // stagnation: the best worst-residual of each patch and the outer
+  // iteration that last improved it by 10%; FP32 vectors put a floor of a
+  // few 1e-7 under the residual, and a tolerance below it would otherwise
+  // run to the matvec cap
+  std::vector<double> best_res(np, 1e300);
+  std::vector<int> best_at(np, 0);
+  constexpr int kStagnant = 4, kMaxOuter = 400;
   float* X = lv.blk[0];
   float* Y = lv.blk[1];
   float* Z = lv.blk[2];
@@ -1011,7 +1019,12 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
         return GPB_ERR_INTERNAL;
       }
       const bool conv = worst <= tol;
-      if (conv || mv[i] + (long)(deg + 1) * kBlk > q.eig_max_matvecs) {
+      if (worst < 0.9 * best_res[i]) {
+        best_res[i] = worst;
+        best_at[i] = outer;
+      }
+      const bool stalled = outer - best_at[i] >= kStagnant;
+      if (conv || stalled || outer >= kMaxOuter || mv[i] + (long)(deg + 1) * kBlk > q.eig_max_matvecs) {
         active[i] = 0;
         done[i] = 1;
         maxres = std::max(maxres, (float)worst);
@@ -1071,7 +1084,6 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     st = rr(X, AX);
     if (st != GPB_OK) return st;
     outer++;
-    if (outer > 200) break;
   }
   *Xout = X;
   if (extract) {
@@ -1428,6 +1440,61 @@ extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst
       return GPB_ERR_ARG;
   }
   return e == cudaSuccess ? GPB_OK : GPB_ERR_CUDA;
+}
+
+// Whole-image planes from the last batch's patches (Pieces2Gpb,
+// src/utilities.cpp:180-213, on the device)
+extern "C" gpb_status gpb_stitch_device(gpb_ctx* ctx, int mode, uint32_t width, uint32_t height,
+                                        const gpb_place* places, size_t n, int ramp, float* d_nmax,
+                                        float* d_orient) {
+  if (!ctx || !places || !d_nmax || !d_orient || width == 0 || height == 0) return GPB_ERR_ARG;
+  if (mode < GPB_STITCH_LAST || mode > GPB_STITCH_BLEND) return GPB_ERR_ARG;
+  if (n == 0 || n != ctx->patches.size()) {
+    ctx->last_error = "place count differs from the last batch";
+    return GPB_ERR_ARG;
+  }
+  for (size_t i = 0; i < n; i++) {
+    const gpb_place& q = places[i];
+    const PatchDev& P = ctx->patches[i];
+    if (q.ix < 0 || q.iy < 0 || q.iw < 0 || q.ih < 0 || q.ix + q.iw > P.W || q.iy + q.ih > P.H) return GPB_ERR_ARG;
+  }
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->st;
+  Buf& b = ctx->b;
+  const int colmajor = ctx->prm.compat == GPB_COMPAT_DAMASCENE;
+  const long long plane = (long long)width * height;
+  if (mode == GPB_STITCH_BLEND) {
+    CK(grow(b.stitch, b.c_stitch, 10 * (size_t)plane));
+    CK(cudaMemsetAsync(b.stitch, 0, 10 * (size_t)plane * sizeof(float), s));
+  }
+  const float rmp = (float)(ramp > 0 ? ramp : 10);
+  for (size_t i = 0; i < n; i++) {
+    const gpb_place& q = places[i];
+    const PatchDev& P = ctx->patches[i];
+    StitchBox bx;
+    bx.ox = q.x0;
+    bx.oy = q.y0;
+    if (mode == GPB_STITCH_INTERIOR) {
+      bx.x = q.ix;
+      bx.y = q.iy;
+      bx.w = q.iw;
+      bx.h = q.ih;
+    } else {
+      bx.x = 0;
+      bx.y = 0;
+      bx.w = P.W;
+      bx.h = P.H;
+    }
+    if (mode == GPB_STITCH_BLEND)
+      CK(launch_stitch_acc(b.patches, (int)i, P.N, b.nmax, b.orient, colmajor, bx, (int)width, (int)height, rmp,
+                           b.stitch, s));
+    else
+      CK(launch_stitch_copy(b.patches, (int)i, b.nmax, b.orient, colmajor, bx, (int)width, (int)height, d_nmax,
+                            d_orient, s));
+  }
+  if (mode == GPB_STITCH_BLEND) CK(launch_stitch_norm(b.stitch, plane, d_nmax, d_orient, s));
+  CK(cudaStreamSynchronize(s));
+  return GPB_OK;
 }
 
 // Texton labels of one device-resident image without allocating: the

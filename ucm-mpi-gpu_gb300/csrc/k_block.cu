@@ -632,7 +632,11 @@ __global__ void __launch_bounds__(256) cf_coarse_norm(CoarseArgs c) {
   }
 }
 
-// fine start block from the coarse Ritz vectors: y = D^1/2 P D_c^-1/2 y_c
+// fine start block from the coarse Ritz vectors: the coarse generalised
+// eigenvectors u_c = D_c^-1/2 y_c interpolated bilinearly to the fine pixel
+// centres (clamped at the patch border), then y = D^1/2 u.  Smoother than
+// the piecewise-constant P u_c of the Galerkin pair, so the fine level
+// starts closer to its eigenvectors.
 __global__ void __launch_bounds__(256) cf_prolong(CoarseArgs c, const float* __restrict__ xc,
                                                   float* __restrict__ xf) {
   const int4 w = c.work_f[blockIdx.x];  // fine (patch, y0, x0)
@@ -640,17 +644,30 @@ __global__ void __launch_bounds__(256) cf_prolong(CoarseArgs c, const float* __r
   const int y = w.y + threadIdx.x / 16, x = w.z + threadIdx.x % 16;
   if (y >= F.H || x >= F.W) return;
   const long long p = F.vec + (long long)y * F.W + x;
-  const long long P = C.vec + (long long)(y >> 1) * C.W + (x >> 1);
-  const float s = sqrtf(c.deg[p]) * c.disc[P];
-  const float4* src = (const float4*)(xc + P * kBlk);
+  // fine centre in coarse pixel coordinates
+  const float cy = fminf(fmaxf((y + 0.5f) * 0.5f - 0.5f, 0.f), (float)(C.H - 1));
+  const float cx = fminf(fmaxf((x + 0.5f) * 0.5f - 0.5f, 0.f), (float)(C.W - 1));
+  const int y0 = (int)cy, x0 = (int)cx;
+  const int y1 = min(y0 + 1, C.H - 1), x1 = min(x0 + 1, C.W - 1);
+  const float fy = cy - y0, fx = cx - x0;
+  const long long P00 = C.vec + (long long)y0 * C.W + x0, P01 = C.vec + (long long)y0 * C.W + x1;
+  const long long P10 = C.vec + (long long)y1 * C.W + x0, P11 = C.vec + (long long)y1 * C.W + x1;
+  const float sq = sqrtf(c.deg[p]);
+  const float w00 = (1.f - fy) * (1.f - fx) * c.disc[P00] * sq, w01 = (1.f - fy) * fx * c.disc[P01] * sq;
+  const float w10 = fy * (1.f - fx) * c.disc[P10] * sq, w11 = fy * fx * c.disc[P11] * sq;
+  const float4* a = (const float4*)(xc + P00 * kBlk);
+  const float4* b = (const float4*)(xc + P01 * kBlk);
+  const float4* cc = (const float4*)(xc + P10 * kBlk);
+  const float4* d = (const float4*)(xc + P11 * kBlk);
   float4* dst = (float4*)(xf + p * kBlk);
 #pragma unroll
   for (int c4 = 0; c4 < kBlk / 4; c4++) {
-    float4 v = src[c4];
-    v.x *= s;
-    v.y *= s;
-    v.z *= s;
-    v.w *= s;
+    const float4 va = a[c4], vb = b[c4], vc = cc[c4], vd = d[c4];
+    float4 v;
+    v.x = w00 * va.x + w01 * vb.x + w10 * vc.x + w11 * vd.x;
+    v.y = w00 * va.y + w01 * vb.y + w10 * vc.y + w11 * vd.y;
+    v.z = w00 * va.z + w01 * vb.z + w10 * vc.z + w11 * vd.z;
+    v.w = w00 * va.w + w01 * vb.w + w10 * vc.w + w11 * vd.w;
     dst[c4] = v;
   }
 }

@@ -49,4 +49,17 @@ cudaError_t launch_spb(const PatchDev* patches, const int4* work, int nwork, con
                        int nvec, const float* go, const float* mpb, int compat, float* spb_out,
                        float* gpbo_out, float* out_nmax, float* out_orient, cudaStream_t s);
 
+// k_stitch.cu: a sub-box (x, y, w, h, patch coordinates) of a patch placed
+// at (ox, oy) in the image
+struct StitchBox {
+  int ox, oy, x, y, w, h;
+};
+cudaError_t launch_stitch_copy(const PatchDev* patches, int pi, const float* nmax, const float* orient, int colmajor,
+                               const StitchBox& bx, int img_w, int img_h, float* out_nmax, float* out_orient,
+                               cudaStream_t s);
+cudaError_t launch_stitch_acc(const PatchDev* patches, int pi, long long npix, const float* nmax, const float* orient,
+                              int colmajor, const StitchBox& bx, int img_w, int img_h, float ramp, float* acc,
+                              cudaStream_t s);
+cudaError_t launch_stitch_norm(const float* acc, long long plane, float* out_nmax, float* out_orient, cudaStream_t s);
+
 }  // namespace gpb

@@ -20,6 +20,7 @@ LIBPATH = os.path.join(_HERE, "libgpb.so")
 (GPB_OK, GPB_ERR_ARG, GPB_ERR_CUDA, GPB_ERR_NOMEM, GPB_ERR_NOCONV, GPB_ERR_TIMEOUT, GPB_ERR_INTERNAL,
  GPB_ERR_TOO_LARGE) = range(8)
 STATIC_MAX_PIXELS = 1 << 20   # gpb_texton_labels_static's scratch limit
+STITCH_LAST, STITCH_INTERIOR, STITCH_BLEND = 0, 1, 2
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
 EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
@@ -96,6 +97,8 @@ def _lib():
         L.gpb_status_str.argtypes = [c]
         L.gpb_status_str.restype = ctypes.c_char_p
         L.gpb_free.argtypes = [vp]
+        L.gpb_stitch_device.argtypes = [vp, c, ctypes.c_uint32, ctypes.c_uint32, vp, sz, c, vp, vp]
+        L.gpb_stitch_device.restype = c
         L.gpb_texton_labels_static.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
         L.gpb_texton_labels_static.restype = c
         _L = L
@@ -186,6 +189,14 @@ class Context:
         out = np.empty(shape, dtype)
         _check(_lib().gpb_fetch(self._h, STAGES[stage], patch, out.ctypes.data, out.nbytes), "gpb_fetch")
         return out
+
+    def stitch_device(self, mode, width, height, places, d_nmax, d_orient, ramp=0):
+        """gpb_stitch_device: whole-image planes (device pointers d_nmax,
+        d_orient) from the last batch; places = [(x0, y0, ix, iy, iw, ih)] per
+        patch, in batch order."""
+        arr = np.ascontiguousarray(np.asarray(places, np.int32).reshape(-1, 6))
+        _check(_lib().gpb_stitch_device(self._h, mode, width, height, arr.ctypes.data, arr.shape[0], ramp,
+                                        d_nmax, d_orient), "gpb_stitch_device")
 
     def texton_labels_static(self, width, height, d_packed, d_labels, stream=None):
         """gpb_texton_labels_static: labels (L | a<<8 | b<<16 | texton<<24)
