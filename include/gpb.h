@@ -70,6 +70,9 @@ typedef struct {
   int keep_intermediates;/* 1: retain per-stage buffers for gpb_fetch(); 2: also counts */
   int cheb_degree;       /* Chebyshev filter degree of the block solver          */
   float warm_tol;        /* residual at which the coarse warm-start solve stops  */
+  float eig_gap_frac;    /* block solvers: a patch also needs residual <= this x
+                            its smallest gap between wanted eigenvalues (floor
+                            1e-7; 0 disables)                                    */
 } gpb_params;
 
 typedef struct gpb_ctx gpb_ctx;

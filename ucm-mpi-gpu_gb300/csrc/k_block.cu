@@ -176,8 +176,14 @@ __device__ __forceinline__ float f4get(const float4& v) {
 // one staged position (RY, DX) relative to the warp's block origin: the value
 // of this lane's column there, times the coefficient of every block pixel
 // whose stencil covers it
-template <class S, int RY, int DX, int I>
-__device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float v, float4 (&cw)[16], float (&acc)[16]) {
+// C (compensated): products rounded to FP32 are summed as a float-float
+// (TwoSum), removing the accumulation error of the 81-term sum -- the term
+// that dominates near an eigenvector, where the diagonal and the
+// off-diagonal sum nearly cancel; used for the Rayleigh-Ritz products and
+// residuals, not the filter
+template <class S, bool C, int RY, int DX, int I>
+__device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float v, float4 (&cw)[16], float (&acc)[16],
+                                            float (&lo)[16]) {
   if constexpr (I < ST_B * ST_B) {
     constexpr int bi = I / ST_B, bj = I % ST_B;
     if constexpr (S::in(RY - bi, DX - bj)) {
@@ -185,15 +191,23 @@ __device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float 
       // a pixel meets its offsets in scanline order, so chunk idx/4 is
       // first needed at idx % 4 == 0
       if constexpr (idx % 4 == 0) cw[I] = *(const float4*)(cs + (bi * ST_TX + bj) * S::NC + idx);
-      acc[I] = fmaf(f4get<idx % 4>(cw[I]), v, acc[I]);
+      if constexpr (C) {
+        const float p = __fmul_rn(f4get<idx % 4>(cw[I]), v);
+        const float s = __fadd_rn(acc[I], p);
+        const float z = s - acc[I];
+        lo[I] += (acc[I] - (s - z)) + (p - z);
+        acc[I] = s;
+      } else {
+        acc[I] = fmaf(f4get<idx % 4>(cw[I]), v, acc[I]);
+      }
     }
-    step_pixels<S, RY, DX, I + 1>(cs, v, cw, acc);
+    step_pixels<S, C, RY, DX, I + 1>(cs, v, cw, acc, lo);
   }
 }
 
-template <class S, int P>
+template <class S, bool C, int P>
 __device__ __forceinline__ void step_positions(const float* __restrict__ ys, const float* __restrict__ cs,
-                                               float4 (&cw)[16], float (&acc)[16]) {
+                                               float4 (&cw)[16], float (&acc)[16], float (&lo)[16]) {
   constexpr int NX = ST_B + 2 * S::R;
   if constexpr (P < NX * NX) {
     constexpr int RY = P / NX - S::R, DX = P % NX - S::R;
@@ -205,9 +219,9 @@ __device__ __forceinline__ void step_positions(const float* __restrict__ ys, con
     }();
     if constexpr (any) {
       const float v = ys[((RY + S::R) * StepSmem<S>::PW + (DX + S::R)) * kBlk];
-      step_pixels<S, RY, DX, 0>(cs, v, cw, acc);
+      step_pixels<S, C, RY, DX, 0>(cs, v, cw, acc, lo);
     }
-    step_positions<S, P + 1>(ys, cs, cw, acc);
+    step_positions<S, C, P + 1>(ys, cs, cw, acc, lo);
   }
 }
 
@@ -221,7 +235,7 @@ __device__ __forceinline__ void step_positions(const float* __restrict__ ys, con
 // a wait that gives up sets *a.err and ends the CTA.
 constexpr int kStepConsumers = 8, kStepThreads = (kStepConsumers + 1) * 32;
 
-template <class S>
+template <class S, bool C>
 __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const int4* __restrict__ work, int nwork,
                                                              const float* __restrict__ Y, const float* __restrict__ X,
                                                              float* __restrict__ out, int step) {
@@ -308,11 +322,15 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
       const int y = m.y0 + by + k / ST_B, x = m.x0 + bx + k % ST_B;
       xr[k] = (m.cz != 0.f && y < m.H && x < m.W) ? X[(m.vec + (long long)y * m.W + x) * kBlk + lane] : 0.f;
     }
-    float acc[16];
+    float acc[16], lo[16];
     float4 cw[16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) acc[k] = 0.f;
-    step_positions<S, 0>(ys + (by * SM::PW + bx) * kBlk + lane, cs + (by * ST_TX + bx) * S::NC, cw, acc);
+    for (int k = 0; k < 16; k++) acc[k] = lo[k] = 0.f;
+    step_positions<S, C, 0>(ys + (by * SM::PW + bx) * kBlk + lane, cs + (by * ST_TX + bx) * S::NC, cw, acc, lo);
+    if constexpr (C) {
+#pragma unroll
+      for (int k = 0; k < 16; k++) acc[k] += lo[k];
+    }
 #pragma unroll
     for (int k = 0; k < 16; k++) {
       const int y = m.y0 + by + k / ST_B, x = m.x0 + bx + k % ST_B;
@@ -365,9 +383,11 @@ __global__ void __launch_bounds__(256) cf_full(const PatchDev* __restrict__ patc
 
 // ------------------------------------------------------------------ Gram
 __device__ __forceinline__ void ffp(float& hi, float& lo, float a, float b) {
-  const float p = a * b;
+  // __fmul_rn / __fadd_rn: never contracted into an FMA, which would break
+  // the error-free transformations
+  const float p = __fmul_rn(a, b);
   const float pe = fmaf(a, b, -p);
-  const float s = hi + p;
+  const float s = __fadd_rn(hi, p);
   const float z = s - hi;
   lo += ((hi - (s - z)) + (p - z)) + pe;
   hi = s;
@@ -461,17 +481,27 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
   }
 }
 
-// U <- U M (and V <- V M if V), M = a.mat[patch] (32 x 32, FP64 on the host,
-// applied in FP32: the next orthonormalisation or Rayleigh-Ritz step absorbs
-// the rounding); one thread per pixel row, M in shared memory
+// U <- U M (and V <- V M if V), M = a.mat[patch] (32 x 32, FP64 on the
+// host), one thread per pixel row.  C (the Rayleigh-Ritz rotation): M is
+// split into FP32 hi + lo parts and each output sums its 32 products as a
+// float-float (TwoProduct by FMA, TwoSum), so the Ritz vectors carry no more
+// than FP32 storage rounding; a plain FP32 sum (enough for the
+// orthonormalisation passes, which the next Rayleigh-Ritz step corrects)
+// leaves ~3e-7 relative error per element.
+template <bool C>
 __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ U, float* __restrict__ V,
                                                  int ncols) {
   const EigTile t = a.tiles[blockIdx.x];
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
-  __shared__ __align__(16) float mh[kBlk][kBlk];
+  __shared__ __align__(16) float mh[kBlk][kBlk], ml[kBlk][kBlk];
   const double* M = a.mat + (long long)t.patch * kBlk * kBlk;
-  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) mh[e / kBlk][e % kBlk] = (float)M[e];
+  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) {
+    const double m = M[e];
+    const float h = (float)m;
+    mh[e / kBlk][e % kBlk] = h;
+    ml[e / kBlk][e % kBlk] = (float)(m - (double)h);
+  }
   __syncthreads();
   for (int p = t.p0 + threadIdx.x; p < t.p1; p += blockDim.x) {
     for (int which = 0; which < (V ? 2 : 1); which++) {
@@ -487,16 +517,28 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
       }
 #pragma unroll 1
       for (int c0 = 0; c0 < kBlk; c0 += 4) {
-        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int r = 0; r < kBlk; r++) {
-          const float4 m4 = *(const float4*)&mh[r][c0];  // broadcast: every thread reads the same row
-          o.x = fmaf(x[r], m4.x, o.x);
-          o.y = fmaf(x[r], m4.y, o.y);
-          o.z = fmaf(x[r], m4.z, o.z);
-          o.w = fmaf(x[r], m4.w, o.w);
+          const float4 h4 = *(const float4*)&mh[r][c0];  // broadcast: every thread reads the same row
+          const float4 l4 = *(const float4*)&ml[r][c0];
+          const float hh[4] = {h4.x, h4.y, h4.z, h4.w}, ll[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            if constexpr (C) {
+              const float pr = __fmul_rn(x[r], hh[j]);  // kept apart from the add below
+              const float pe = fmaf(x[r], hh[j], -pr);  // exact error of the product
+              const float s = __fadd_rn(hi[j], pr);
+              const float z = s - hi[j];
+              lo[j] += ((hi[j] - (s - z)) + (pr - z)) + fmaf(x[r], ll[j], pe);
+              hi[j] = s;
+            } else {
+              hi[j] = fmaf(x[r], hh[j], hi[j]);
+            }
+          }
         }
-        if (c0 < ncols) *(float4*)(row + c0) = o;
+        if (c0 < ncols)
+          *(float4*)(row + c0) = make_float4(hi[0] + lo[0], hi[1] + lo[1], hi[2] + lo[2], hi[3] + lo[3]);
       }
     }
   }
@@ -682,26 +724,41 @@ cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc,
   return cudaGetLastError();
 }
 
+template <class S, bool C>
+static void step_attr() {
+  cudaFuncSetAttribute(cf_step_t<S, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)StepSmem<S>::bytes);
+}
+
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
-                           int step, cudaStream_t s) {
+                           int step, cudaStream_t s, bool comp) {
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(cf_step_t<DiskStencil>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)StepSmem<DiskStencil>::bytes);
-    cudaFuncSetAttribute(cf_step_t<SquareStencil>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)StepSmem<SquareStencil>::bytes);
+    step_attr<DiskStencil, false>();
+    step_attr<DiskStencil, true>();
+    step_attr<SquareStencil, false>();
+    step_attr<SquareStencil, true>();
     if (nsm <= 0) nsm = 1;
   }
   const int grid = std::min(nwork, nsm);  // one persistent CTA per SM
   if (grid <= 0) return cudaSuccess;
-  if (a.coarse)
-    cf_step_t<SquareStencil><<<grid, kStepThreads, StepSmem<SquareStencil>::bytes, s>>>(a, work, nwork, Y, X, out,
-                                                                                      step);
-  else
-    cf_step_t<DiskStencil><<<grid, kStepThreads, StepSmem<DiskStencil>::bytes, s>>>(a, work, nwork, Y, X, out, step);
+  if (a.coarse) {
+    if (comp)
+      cf_step_t<SquareStencil, true><<<grid, kStepThreads, StepSmem<SquareStencil>::bytes, s>>>(a, work, nwork, Y, X,
+                                                                                              out, step);
+    else
+      cf_step_t<SquareStencil, false><<<grid, kStepThreads, StepSmem<SquareStencil>::bytes, s>>>(a, work, nwork, Y, X,
+                                                                                               out, step);
+  } else {
+    if (comp)
+      cf_step_t<DiskStencil, true><<<grid, kStepThreads, StepSmem<DiskStencil>::bytes, s>>>(a, work, nwork, Y, X, out,
+                                                                                          step);
+    else
+      cf_step_t<DiskStencil, false><<<grid, kStepThreads, StepSmem<DiskStencil>::bytes, s>>>(a, work, nwork, Y, X, out,
+                                                                                           step);
+  }
   return cudaGetLastError();
 }
 cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwork, const float* a_up,
@@ -720,8 +777,12 @@ cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const f
   cf_gram<<<ntiles, 256, smem, s>>>(a, U, V, out);
   return cudaGetLastError();
 }
-cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s) {
-  cf_rotate<<<ntiles, 256, 0, s>>>(a, U, V, ncols);
+cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,
+                             bool comp) {
+  if (comp)
+    cf_rotate<true><<<ntiles, 256, 0, s>>>(a, U, V, ncols);
+  else
+    cf_rotate<false><<<ntiles, 256, 0, s>>>(a, U, V, ncols);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const float* AX, double* out,

@@ -56,10 +56,11 @@ void upload_block(const HostTables& t, cudaStream_t s);
 constexpr int kStepTileH = 8, kStepTileW = 16;  // cf_step tile (work list entries)
 constexpr int kFullNC = 84, kCoarseNC = 52;      // floats per pixel-major stencil row
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
-                           int step, cudaStream_t s);
+                           int step, cudaStream_t s, bool comp = false);
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
                            cudaStream_t s);
-cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s);
+cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,
+                             bool comp = false);
 cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const float* AX, double* out,
                             cudaStream_t s);
 cudaError_t cf_launch_extract(const BlkArgs& a, int ntiles, const float* X, float* evec, int nvec,

@@ -43,9 +43,11 @@ void upload_eig(const HostTables& t, cudaStream_t s) {
 constexpr unsigned FULLM = 0xffffffffu;
 
 __device__ __forceinline__ void ff_add_prod(float& hi, float& lo, float a, float b) {
-  const float p = a * b;
+  // __fmul_rn / __fadd_rn: never contracted into an FMA, which would break
+  // the error-free transformations
+  const float p = __fmul_rn(a, b);
   const float pe = fmaf(a, b, -p);
-  const float s = hi + p;
+  const float s = __fadd_rn(hi, p);
   const float z = s - hi;
   const float e = (hi - (s - z)) + (p - z);
   hi = s;

@@ -38,7 +38,8 @@ class Params(ctypes.Structure):
                 ("eig_tol", ctypes.c_float), ("eig_max_matvecs", ctypes.c_int),
                 ("krylov_dim", ctypes.c_int), ("krylov_keep", ctypes.c_int),
                 ("eig_mode", ctypes.c_int), ("keep_intermediates", ctypes.c_int),
-                ("cheb_degree", ctypes.c_int), ("warm_tol", ctypes.c_float)]
+                ("cheb_degree", ctypes.c_int), ("warm_tol", ctypes.c_float),
+                ("eig_gap_frac", ctypes.c_float)]
 
 
 class Patch(ctypes.Structure):
