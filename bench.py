@@ -29,12 +29,12 @@ sys.path.insert(0, os.path.join(ROOT, "ucm-mpi-gpu_gb300"))
 import numpy as np  # noqa: E402
 
 METRIC = "gPb Mpix/s on 1 GB300: warm-started vs plain Lanczos, eig residual <=1e-4"
-WORKLOAD = "config2: 1024x1024 Voronoi(256 cells, sigma 8) -> 16 x 256^2 patches + 5-px halo, one batch"
+WORKLOAD = "1024x1024 Voronoi(256 cells, sigma 8) -> 16 x 256^2 patches + 5-px halo, one batch"
 
 
 def make_workload():
     from gpb import synth
-    img, cb = synth.config2()
+    img, cb = synth.image_1024()
     boxes = synth.grid_patches(1024, 1024, 4, 4, 5)
     patches = [np.ascontiguousarray(synth.pack_bgr(img[y0:y0 + h, x0:x0 + w]))
                for (y0, x0, h, w, *_r) in boxes]

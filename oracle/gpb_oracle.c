@@ -380,8 +380,8 @@ int orc_hist_gradient(const uint8_t* lab, int Hp, int Wp, int border, int r, con
   return nb;
 }
 
-/* mex_pb_parts_final_selected.cpp:76-235 with BASELINE's Schmid-codebook
- * textons in place of k-means (D8): mirror 30, Lab quantised to 25 bins,
+/* mex_pb_parts_final_selected.cpp:76-235 with the Schmid-codebook textons
+ * (genTextonMap, src/SPFeatures.cpp:277-360) in place of k-means (D8): mirror 30, Lab quantised to 25 bins,
  * bg r={3,5,10} (sigma 0.1*25), cga/cgb r={5,10,20} (sigma 0.05*25),
  * tg r={5,10,20} on the mirrored texton map, unsmoothed. */
 void orc_local_cues(const uint8_t* bgr, const uint8_t* texton, int H, int W, const orc_params* p,

@@ -144,11 +144,11 @@ def test_gpb_small_both_solvers(small, mode):
 
 
 @pytest.mark.parametrize("mode", [0, 1])
-def test_gpb_config1(orc, mode):
+def test_gpb_single_patch_321x481(orc, mode):
     """321 x 481, 24 cells: the reference's single-patch case."""
     import gpb
     from gpb import synth
-    img, cb = synth.config1()
+    img, cb = synth.image_321x481()
     ref = orc.globalpb(img, cb)
     ctx = gpb.Context(cb, eig_mode=mode, keep_intermediates=1)
     orient, nmax = gpb.GlobalPbCuda(ctx, img)
@@ -284,13 +284,13 @@ def test_computeGPb_shim(small):
     ctx.close()
 
 
-def test_config2_batch_properties(orc):
+def test_batch_1024_sixteen_patches(orc):
     """The benchmark workload (16 halo'd patches of a 1024^2 image, one batch):
     every patch converges, eigen-residuals hold in FP64, and two patches match
     the full oracle within the gPb tolerance."""
     import gpb
     from gpb import synth
-    img, cb = synth.config2()
+    img, cb = synth.image_1024()
     boxes = synth.grid_patches(1024, 1024, 4, 4, 5)
     patches = [synth.pack_bgr(img[y0:y0 + h, x0:x0 + w]) for (y0, x0, h, w, *_r) in boxes]
     ctx = gpb.Context(cb, keep_intermediates=1, eig_mode=gpb.EIG_WARM)
@@ -307,14 +307,14 @@ def test_config2_batch_properties(orc):
     ctx.close()
 
 
-def test_config3_uneven_batch(orc):
+def test_batch_4096_uneven_patches(orc):
     """64 rectangles with sides in [200, 700] of a 4096^2 image (4096 cells,
     sigma 6, 40 lines), one warm-started batch: every patch converges, the
     outputs are finite gPb maps, and the two smallest patches match their own
     oracle runs within the gPb tolerance."""
     import gpb
     from gpb import synth
-    img, cb, boxes = synth.config3()
+    img, cb, boxes = synth.image_4096_uneven()
     crops = [np.ascontiguousarray(img[y0:y0 + h, x0:x0 + w]) for (y0, x0, h, w) in boxes]
     ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
     outs = ctx.compute_batch([synth.pack_bgr(c) for c in crops])

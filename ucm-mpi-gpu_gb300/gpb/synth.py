@@ -129,13 +129,13 @@ def pack_bgr(bgr):
 
 
 # ------------------------------------------------------------ named workloads
-def config1():
+def image_321x481():
     """321 x 481, 24 cells, sigma 8: one patch."""
     img = voronoi_image(321, 481, 24, 8.0, SEED_BASE + 1)
     return img, make_codebook(img, SEED_BASE + 1)
 
 
-def config2():
+def image_1024():
     """1024 x 1024, 256 cells, sigma 8: 16 x 256^2 patches with a 5-px halo."""
     img = voronoi_image(1024, 1024, 256, 8.0, SEED_BASE + 2)
     return img, make_codebook(img, SEED_BASE + 2)
@@ -157,7 +157,7 @@ def grid_patches(H, W, rows, cols, halo):
     return out
 
 
-def config3():
+def image_4096_uneven():
     """4096 x 4096, 4096 cells, sigma 6, 40 lines: the uneven-batching image.
     Returns (image, codebook, boxes) with 64 rectangles whose sides are uniform
     in [200, 700] px at uniform positions, as (y0, x0, h, w)."""
@@ -171,7 +171,7 @@ def config3():
     return img, make_codebook(img, SEED_BASE + 3), boxes
 
 
-def config5():
+def image_8192():
     """8192 x 8192, 16384 cells, sigma 8, 200 lines: 256 patches of 512^2 with
     a 5-px halo (grid_patches(8192, 8192, 16, 16, 5))."""
     img = voronoi_image(8192, 8192, 16384, 8.0, SEED_BASE + 5, lines=200)
