@@ -179,6 +179,22 @@ typedef struct {
 gpb_status gpb_stitch_device(gpb_ctx* ctx, int mode, uint32_t width, uint32_t height, const gpb_place* places,
                              size_t n, int ramp, float* d_nmax, float* d_orient);
 
+/* Per-superpixel descriptors for GLSVM (SPFeatures, src/SPFeatures.cpp) of
+ * patch `patch` of the last compute call, from that call's texton map, grey
+ * image and input colours.  d_labels: the patch's superpixel map (W*H int32,
+ * row-major, device); pixels whose label is outside [0, n_labels) are
+ * skipped.  d_out (device, n_labels rows of doubles) receives per row
+ *   [ texton histogram (K columns, only if with_textons) |
+ *     grey-level histogram, bin = grey / bin_step (255 / bin_step + 1 columns) |
+ *     0 (the Harris corner descriptor's column, not computed) |
+ *     mean B, G, R ]
+ * histograms divided by the superpixel's size and multiplied by 10, means
+ * multiplied by 10/255 (genTextonFeatures :260-275, genIntensityHistograms
+ * :101-114, genAverageFeatures :380-391); rows of empty superpixels are zero.
+ * Synchronous on the context's stream. */
+gpb_status gpb_superpixel_features(gpb_ctx* ctx, size_t patch, const int32_t* d_labels, int32_t n_labels,
+                                   int bin_step, int with_textons, double* d_out);
+
 /* Texton and Lab-bin labels of one image already on the device, computed
  * without allocating memory, on the device or the host.  No counterpart in
  * the reference: its texton stage (src/SPFeatures.cpp:277-360) allocates

@@ -311,3 +311,39 @@ def ref_spectra(rowptr, cols, vals, nev, ncv):
     vec = np.zeros((nev, n), np.float64)
     nc = ref().ref_spectra_geigs(n, rowptr, cols, vals, nev, ncv, ev, vec)
     return nc, ev, vec
+
+
+def superpixel_features(bgr, texton, labels, n_labels, bin_step, K=None):
+    """SPFeatures' per-superpixel rows (src/SPFeatures.cpp): texton histogram
+    (genTextonFeatures pooling :260-275, only if K), grey-level histogram with
+    bin = grey / bin_step (genIntensityHistograms :101-114), a zero column for
+    the corner descriptor, mean B, G, R (genAverageFeatures :380-391);
+    histograms / size * 10, means / size * (10 / 255), in that order."""
+    grey = grey_bgr(bgr).astype(np.int64)
+    nbins = 255 // bin_step + 1
+    K = K or 0
+    out = np.zeros((n_labels, K + nbins + 4), np.float64)
+    lab = labels.ravel()
+    ok = (lab >= 0) & (lab < n_labels)
+    l = lab[ok]
+    size = np.bincount(l, minlength=n_labels).astype(np.float64)
+    cols = []
+    if K:
+        cols.append(np.zeros((n_labels, K)))
+        np.add.at(cols[-1], (l, texton.ravel()[ok].astype(np.int64)), 1)
+    hist = np.zeros((n_labels, nbins))
+    np.add.at(hist, (l, grey.ravel()[ok] // bin_step), 1)
+    cols.append(hist)
+    nz = size > 0
+    c0 = 0
+    for c in cols:
+        w = c.shape[1]
+        out[nz, c0:c0 + w] = (c[nz] / size[nz][:, None]) * 10.0
+        c0 += w
+    c0 += 1  # the corner column stays zero
+    px = bgr.reshape(-1, 3)[ok].astype(np.int64)
+    for j in range(3):
+        sm = np.zeros(n_labels)
+        np.add.at(sm, l, px[:, j])
+        out[nz, c0 + j] = (sm[nz] / size[nz]) * (10.0 / 255.0)
+    return out

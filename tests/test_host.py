@@ -91,3 +91,25 @@ def test_spb_orientation_follows_local_cues(orc):
     spb = orc.spb(np.array([0.0, 0.5]), np.stack([np.ones(H * W), v.ravel()]), np.ones(H * W), H, W, 2)
     y, x = H // 2, W // 2
     assert int(np.argmax(cues[:, y, x])) == int(np.argmax(spb[:, y, x]))
+
+
+def test_superpixel_features_oracle_known_answer(orc):
+    """The SPFeatures restatement on a hand-checked 2 x 3 case: two
+    superpixels, one skipped pixel (label -1), bin_step 128 (2 grey bins)."""
+    bgr = np.array([[[0, 0, 0], [255, 255, 255], [10, 20, 30]],
+                    [[255, 255, 255], [0, 0, 0], [1, 2, 3]]], np.uint8)
+    texton = np.array([[0, 1, 1], [2, 0, 0]], np.uint8)
+    labels = np.array([[0, 0, 1], [1, 0, -1]], np.int32)
+    out = orc.superpixel_features(bgr, texton, labels, 2, 128, K=3)
+    grey = orc.grey_bgr(bgr)
+    assert out.shape == (2, 3 + 2 + 4)
+    # superpixel 0: pixels (0,0) black, (0,1) white, (1,1) black; textons 0, 1, 0
+    np.testing.assert_array_equal(out[0, :3], np.array([2, 1, 0]) / 3 * 10)
+    np.testing.assert_array_equal(out[0, 3:5], np.array([2, 1]) / 3 * 10)
+    assert out[0, 5] == 0
+    np.testing.assert_allclose(out[0, 6:], np.array([255, 255, 255]) / 3 * (10 / 255))
+    # superpixel 1: (0,2) and (1,0); textons 1 and 2
+    np.testing.assert_array_equal(out[1, :3], np.array([0, 1, 1]) / 2 * 10)
+    assert grey[0, 2] < 128 <= grey[1, 0]
+    np.testing.assert_array_equal(out[1, 3:5], np.array([1, 1]) / 2 * 10)
+    np.testing.assert_allclose(out[1, 6:], np.array([10 + 255, 20 + 255, 30 + 255]) / 2 * (10 / 255))

@@ -129,6 +129,8 @@ struct Buf {
   float* afull = nullptr; size_t c_afull = 0;  // pixel-major fine stencil rows
   int4* work_act = nullptr; size_t c_wact = 0;  // block-step tiles of the still active patches
   float* stitch = nullptr; size_t c_stitch = 0;  // BLEND accumulators [10][image]
+  uint32_t* spcount = nullptr; size_t c_spcount = 0;          // superpixel histograms
+  unsigned long long* spcsum = nullptr; size_t c_spcsum = 0;  // superpixel colour sums
   int* berr = nullptr; size_t c_berr = 0;
 };
 
@@ -445,7 +447,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
                   b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
                   b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
                   b.bcoef, b.bdone, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk,
-                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr, b.work_act, b.stitch};
+                  b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr, b.work_act, b.stitch, b.spcount, b.spcsum};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
@@ -1509,6 +1511,24 @@ extern "C" gpb_status gpb_stitch_device(gpb_ctx* ctx, int mode, uint32_t width, 
                             d_orient, s));
   }
   if (mode == GPB_STITCH_BLEND) CK(launch_stitch_norm(b.stitch, plane, d_nmax, d_orient, s));
+  CK(cudaStreamSynchronize(s));
+  return GPB_OK;
+}
+
+// Superpixel descriptors of one patch of the last batch (SPFeatures,
+// src/SPFeatures.cpp:101-114, 260-275, 380-391, on the device)
+extern "C" gpb_status gpb_superpixel_features(gpb_ctx* ctx, size_t patch, const int32_t* d_labels, int32_t n_labels,
+                                              int bin_step, int with_textons, double* d_out) {
+  if (!ctx || !d_labels || !d_out || n_labels <= 0 || bin_step < 1 || bin_step > 255) return GPB_ERR_ARG;
+  if (patch >= ctx->patches.size()) return GPB_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->st;
+  Buf& b = ctx->b;
+  const int K = with_textons ? ctx->K : 0, nbins = 255 / bin_step + 1;
+  CK(grow(b.spcount, b.c_spcount, (size_t)n_labels * (K + nbins + 1)));
+  CK(grow(b.spcsum, b.c_spcsum, (size_t)n_labels * 3));
+  CK(launch_sp_features(b.patches, (int)patch, ctx->patches[patch].N, d_labels, n_labels, b.lab4, b.grey, b.packed,
+                        bin_step, K, nbins, b.spcount, b.spcsum, d_out, s));
   CK(cudaStreamSynchronize(s));
   return GPB_OK;
 }

@@ -62,4 +62,10 @@ cudaError_t launch_stitch_acc(const PatchDev* patches, int pi, long long npix, c
                               cudaStream_t s);
 cudaError_t launch_stitch_norm(const float* acc, long long plane, float* out_nmax, float* out_orient, cudaStream_t s);
 
+// k_spfeat.cu
+cudaError_t launch_sp_features(const PatchDev* patches, int pi, long long npix, const int32_t* labels, int n,
+                               const uint32_t* lab4, const uint8_t* grey, const uint32_t* packed, int bin_step,
+                               int K, int nbins, uint32_t* counts, unsigned long long* csum, double* out,
+                               cudaStream_t s);
+
 }  // namespace gpb

@@ -100,6 +100,8 @@ def _lib():
         L.gpb_free.argtypes = [vp]
         L.gpb_stitch_device.argtypes = [vp, c, ctypes.c_uint32, ctypes.c_uint32, vp, sz, c, vp, vp]
         L.gpb_stitch_device.restype = c
+        L.gpb_superpixel_features.argtypes = [vp, sz, vp, ctypes.c_int32, c, c, vp]
+        L.gpb_superpixel_features.restype = c
         L.gpb_texton_labels_static.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
         L.gpb_texton_labels_static.restype = c
         _L = L
@@ -198,6 +200,12 @@ class Context:
         arr = np.ascontiguousarray(np.asarray(places, np.int32).reshape(-1, 6))
         _check(_lib().gpb_stitch_device(self._h, mode, width, height, arr.ctypes.data, arr.shape[0], ramp,
                                         d_nmax, d_orient), "gpb_stitch_device")
+
+    def superpixel_features(self, patch, d_labels, n_labels, d_out, bin_step=8, with_textons=True):
+        """gpb_superpixel_features: n_labels rows of [texton histogram |
+        grey histogram | 0 | mean B G R] into the device doubles at d_out."""
+        _check(_lib().gpb_superpixel_features(self._h, patch, d_labels, n_labels, bin_step, int(with_textons), d_out),
+               "gpb_superpixel_features")
 
     def texton_labels_static(self, width, height, d_packed, d_labels, stream=None):
         """gpb_texton_labels_static: labels (L | a<<8 | b<<16 | texton<<24)
