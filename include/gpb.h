@@ -195,6 +195,14 @@ gpb_status gpb_stitch_device(gpb_ctx* ctx, int mode, uint32_t width, uint32_t he
 gpb_status gpb_superpixel_features(gpb_ctx* ctx, size_t patch, const int32_t* d_labels, int32_t n_labels,
                                    int bin_step, int with_textons, double* d_out);
 
+/* The reference's per-piece files (src/main.cpp:444-452), from host planes:
+ * a rows x cols row-major matrix as an OpenCV FileStorage YAML matrix named
+ * `name` with dt d (OpenCVFileWriter, src/utilities.cpp:33-37; values with
+ * 17 significant digits), and as an 8-bit greyscale PNG scaled min..max to
+ * 0..255 with round-to-nearest-even (OpenCVImageWriter, :21-31). */
+gpb_status gpb_write_yml(const char* path, const char* name, const float* data, uint32_t rows, uint32_t cols);
+gpb_status gpb_write_png_minmax(const char* path, const float* data, uint32_t rows, uint32_t cols);
+
 /* Texton and Lab-bin labels of one image already on the device, computed
  * without allocating memory, on the device or the host.  No counterpart in
  * the reference: its texton stage (src/SPFeatures.cpp:277-360) allocates

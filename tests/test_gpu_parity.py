@@ -331,3 +331,22 @@ def test_batch_4096_uneven_patches(orc):
         assert np.abs(outs[i][0] - ref["nmax"]).max() < GPB_TOL
         assert np.abs(outs[i][1].reshape(8, h, w) - ref["gpb_o"]).max() < GPB_TOL
     ctx.close()
+
+
+def test_codebook_yml_round_trip(tmp_path):
+    """A codebook written with gpb_write_yml and read with
+    gpb_load_codebook_yml gives the same textons as gpb_set_codebook."""
+    import gpb
+    from gpb import synth
+    img, cb = _img(48, 64, 5, 81)
+    p = str(tmp_path / "texton_codebook.yml")
+    c = np.ascontiguousarray(cb, np.float32)
+    assert gpb._lib().gpb_write_yml(p.encode(), b"texton_codebook", c.ctypes.data, c.shape[0], c.shape[1]) == 0
+    a = gpb.Context(cb, keep_intermediates=1)
+    b = gpb.Context(keep_intermediates=1)
+    b.load_codebook_yml(p)
+    a.compute_batch([synth.pack_bgr(img)])
+    b.compute_batch([synth.pack_bgr(img)])
+    assert np.array_equal(a.fetch("texton", 0, (48, 64), np.uint8), b.fetch("texton", 0, (48, 64), np.uint8))
+    a.close()
+    b.close()

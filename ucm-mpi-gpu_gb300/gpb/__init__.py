@@ -100,6 +100,10 @@ def _lib():
         L.gpb_free.argtypes = [vp]
         L.gpb_stitch_device.argtypes = [vp, c, ctypes.c_uint32, ctypes.c_uint32, vp, sz, c, vp, vp]
         L.gpb_stitch_device.restype = c
+        L.gpb_write_yml.argtypes = [ctypes.c_char_p, ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.c_uint32]
+        L.gpb_write_yml.restype = c
+        L.gpb_write_png_minmax.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint32, ctypes.c_uint32]
+        L.gpb_write_png_minmax.restype = c
         L.gpb_superpixel_features.argtypes = [vp, sz, vp, ctypes.c_int32, c, c, vp]
         L.gpb_superpixel_features.restype = c
         L.gpb_texton_labels_static.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
@@ -219,6 +223,22 @@ class Context:
         s = Stats()
         _check(_lib().gpb_last_stats(self._h, ctypes.byref(s)), "gpb_last_stats")
         return s.as_dict()
+
+
+def write_piece_files(prefix, nmax, orient):
+    """The reference's per-piece files (src/main.cpp:444-452) from host
+    planes: <prefix>_gpb_nmax.png and .yml (matrix "gpb_nonmax") and
+    <prefix>_gpb_orient_<o>.png for the 8 orientation planes."""
+    nm = np.ascontiguousarray(nmax, np.float32)
+    H, W = nm.shape
+    ori = np.ascontiguousarray(orient, np.float32).reshape(8, H, W)
+    L = _lib()
+    _check(L.gpb_write_png_minmax((prefix + "_gpb_nmax.png").encode(), nm.ctypes.data, H, W), "gpb_write_png_minmax")
+    _check(L.gpb_write_yml((prefix + "_gpb_nmax.yml").encode(), b"gpb_nonmax", nm.ctypes.data, H, W), "gpb_write_yml")
+    for o in range(8):
+        plane = np.ascontiguousarray(ori[o])
+        _check(L.gpb_write_png_minmax(("%s_gpb_orient_%d.png" % (prefix, o)).encode(), plane.ctypes.data, H, W),
+               "gpb_write_png_minmax")
 
 
 def compute_gpb(ctx, packed):
