@@ -321,7 +321,7 @@ extern "C" void gpb_default_params(gpb_params* p) {
   p->compat = GPB_COMPAT_CPU;
   p->nvec = 9;
   p->eig_tol = 1e-6f;
-  p->eig_max_matvecs = 100000;
+  p->eig_max_matvecs = 200000;
   p->krylov_dim = 40;
   p->krylov_keep = 26;
   p->eig_mode = GPB_EIG_LANCZOS;
@@ -934,12 +934,13 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   std::vector<float> evals((size_t)np * nev, 0.f);
   std::vector<long> mv(np, 0);
   // stagnation: the best worst-residual of each patch and the outer
-  // iteration that last improved it by 10%; FP32 vectors put a floor of a
+  // iteration that last improved it by 2%; FP32 vectors put a floor of a
   // few 1e-7 under the residual, and a tolerance below it would otherwise
-  // run to the matvec cap
+  // run to the matvec cap (a clustered spectrum still converging slowly
+  // gains a few % per outer iteration, so the window is 6)
   std::vector<double> best_res(np, 1e300);
   std::vector<int> best_at(np, 0);
-  constexpr int kStagnant = 4, kMaxOuter = 400;
+  constexpr int kStagnant = 6, kMaxOuter = 400;
   float* X = lv.blk[0];
   float* Y = lv.blk[1];
   float* Z = lv.blk[2];
@@ -1034,7 +1035,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
         tol_i = std::min(tol, std::max(1e-7, q.eig_gap_frac * gmin));
       }
       const bool conv = worst <= tol_i;
-      if (worst < 0.9 * best_res[i]) {
+      if (worst < 0.98 * best_res[i]) {
         best_res[i] = worst;
         best_at[i] = outer;
       }
@@ -1043,9 +1044,12 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
         active[i] = 0;
         done[i] = 1;
         maxres = std::max(maxres, (float)worst);
-        // the gap target is pursued as far as FP32 allows; only a residual
-        // above the requested tolerance is a failure to converge
-        if (!conv && worst > tol) noconv = true;
+        // the gap target is pursued as far as FP32 allows.  FP32 vectors put
+        // a floor under the residual that grows with the patch (about 6e-7
+        // at 0.3 Mpix, 1e-6 at 1.6 Mpix): a patch that stops improving
+        // within 4x the requested tolerance has converged as far as it can;
+        // only a residual above that is a failure to converge
+        if (!conv && worst > 4 * tol) noconv = true;
         for (int c = 0; c < nev; c++) evals[(size_t)i * nev + c] = (float)theta[(size_t)i * kBlk + c];
         continue;
       }
