@@ -222,6 +222,8 @@ struct gpb_ctx {
   // pinned staging
   uint32_t* h_packed = nullptr; size_t c_hpacked = 0;
   float* h_out = nullptr; size_t c_hout = 0;
+  // pinned host staging of the block solvers' small per-patch matrices
+  void* h_small = nullptr; size_t c_hsmall = 0;
   cudaEvent_t ev[12];
   // optional per-kernel timing of the eigensolver launches
   bool profile = false;
@@ -304,6 +306,9 @@ static cudaError_t load_tables(gpb_ctx* ctx) {
   ConstBank& bk = bank_of(ctx->device);
   if (bk.owner == ctx->token) return cudaSuccess;
   cudaStream_t s = ctx->st;
+  // the uploads report through cudaGetLastError: clear an earlier,
+  // unrelated non-sticky error first so it is not taken for theirs
+  (void)cudaGetLastError();
   upload_front(ctx->tab, s);
   upload_cues(ctx->tab, s);
   upload_buildw(ctx->tab, s);
@@ -452,6 +457,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
     if (q) cudaFree(q);
   if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
   if (ctx->h_out) cudaFreeHost(ctx->h_out);
+  if (ctx->h_small) cudaFreeHost(ctx->h_small);
   for (int i = 0; i < 12; i++) cudaEventDestroy(ctx->ev[i]);
   for (cudaEvent_t e : ctx->pev) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -929,8 +935,35 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   a.theta = b.btheta;
   const size_t BB = (size_t)kBlk * kBlk;
   std::vector<int> active(np, 1), done(np, 0);
-  std::vector<double> G(np * BB), M(np * BB), theta(np * (size_t)kBlk, 0.0), res(np * (size_t)kBlk);
-  std::vector<float3> coef(np * (size_t)kMaxCheb);
+  // G, M (32 x 32 per patch), theta, res and the filter coefficients live in
+  // one pinned block, so their copies are direct DMA
+  const size_t nG = np * BB, nT = np * (size_t)kBlk, nC = np * (size_t)kMaxCheb;
+  const size_t need = (2 * nG + 2 * nT) * sizeof(double) + nC * sizeof(float3);
+  if (ctx->c_hsmall < need) {
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    ctx->h_small = nullptr;
+    ctx->c_hsmall = 0;
+    CK(cudaMallocHost(&ctx->h_small, need));
+    ctx->c_hsmall = need;
+  }
+  struct HostArr {  // a span with the operator[] and data() the code below uses
+    double* p;
+    size_t n;
+    double& operator[](size_t i) { return p[i]; }
+    double* data() { return p; }
+    size_t size() const { return n; }
+    double* begin() { return p; }
+  };
+  double* hb = (double*)ctx->h_small;
+  HostArr G{hb, nG}, M{hb + nG, nG}, theta{hb + 2 * nG, nT}, res{hb + 2 * nG + nT, nT};
+  for (size_t i = 0; i < nT; i++) theta[i] = 0.0;
+  struct CoefArr {
+    float3* p;
+    size_t n;
+    float3& operator[](size_t i) { return p[i]; }
+    float3* data() { return p; }
+    size_t size() const { return n; }
+  } coef{(float3*)(hb + 2 * nG + 2 * nT), nC};
   std::vector<float> evals((size_t)np * nev, 0.f);
   std::vector<long> mv(np, 0);
   // stagnation: the best worst-residual of each patch and the outer

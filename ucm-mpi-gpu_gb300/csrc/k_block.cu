@@ -352,32 +352,37 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
 __global__ void __launch_bounds__(256) cf_full(const PatchDev* __restrict__ patches, const int4* __restrict__ work,
                                                const float* __restrict__ a_up, const float* __restrict__ a_diag,
                                                long long lvec, float* __restrict__ afull) {
-  const int4 w = work[blockIdx.x];  // 16 x 16 tile
+  // one thread per pixel of the 16 x 16 tile: the plane reads are coalesced
+  // across the warp, the row goes out as 21 16-byte stores
+  const int4 w = work[blockIdx.x];
   const PatchDev P = patches[w.x];
-  constexpr int NC = DiskStencil::NC;
-  for (int item = threadIdx.x; item < 256 * NC; item += blockDim.x) {
-    const int t = item / NC, e = item % NC;
-    const int y = w.y + t / 16, x = w.z + t % 16;
-    if (y >= P.H || x >= P.W) continue;
-    const long long p = P.vec + (long long)y * P.W + x;
-    float v = 0.f;
-    if (e < kStencilN) {
-      const int ctr = kStencilN / 2;
-      int dy, dx, k;
+  constexpr int NC = DiskStencil::NC, ctr = kStencilN / 2;
+  const int y = w.y + threadIdx.x / 16, x = w.z + threadIdx.x % 16;
+  if (y >= P.H || x >= P.W) return;
+  const long long p = P.vec + (long long)y * P.W + x;
+  float4* row = (float4*)(afull + p * NC);
+#pragma unroll 1
+  for (int e4 = 0; e4 < NC / 4; e4++) {
+    float v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int e = 4 * e4 + j;
+      v[j] = 0.f;
+      if (e >= kStencilN) continue;
       if (e == ctr) {
-        v = a_diag[p];
-      } else {
-        // upper offsets are c_bup[e - 41]; the disk is point-symmetric, so
-        // lower offset e mirrors upper offset 80 - e
-        k = e > ctr ? e - ctr - 1 : kStencilN - 1 - e - ctr - 1;
-        dy = e > ctr ? c_bup_dy[k] : -c_bup_dy[k];
-        dx = e > ctr ? c_bup_dx[k] : -c_bup_dx[k];
-        const int yy = y + dy, xx = x + dx;
-        if (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W)
-          v = e > ctr ? a_up[(long long)k * lvec + p] : a_up[(long long)k * lvec + p + (long long)dy * P.W + dx];
+        v[j] = a_diag[p];
+        continue;
       }
+      // upper offsets are c_bup[e - 41]; the disk is point-symmetric, so
+      // lower offset e mirrors upper offset 80 - e
+      const int k = e > ctr ? e - ctr - 1 : kStencilN - 1 - e - ctr - 1;
+      const int dy = e > ctr ? c_bup_dy[k] : -c_bup_dy[k];
+      const int dx = e > ctr ? c_bup_dx[k] : -c_bup_dx[k];
+      const int yy = y + dy, xx = x + dx;
+      if (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W)
+        v[j] = e > ctr ? a_up[(long long)k * lvec + p] : a_up[(long long)k * lvec + p + (long long)dy * P.W + dx];
     }
-    afull[p * NC + e] = v;
+    row[e4] = make_float4(v[0], v[1], v[2], v[3]);
   }
 }
 
