@@ -216,7 +216,7 @@ __device__ __forceinline__ void cue_combo(const uint8_t* hist, int c, int lane, 
 }
 
 template <bool kRaw>
-__global__ void __launch_bounds__(CT_WARPS * 32) k_cues(const PatchDev* __restrict__ patches,
+__global__ void __launch_bounds__(CT_WARPS * 32, 3) k_cues(const PatchDev* __restrict__ patches,
                                                         const int4* __restrict__ work,
                                                         const uint32_t* __restrict__ lab4,
                                                         const int* __restrict__ nbins,
