@@ -103,6 +103,8 @@ typedef struct {
   double spmv_ms, orth_ms;
   long spmv_launches, orth_launches;
   double spmv_bytes, orth_bytes;
+  int eig_fallback;           /* 1: a block solver missed its target and the batch
+                                 was solved again by plain Lanczos                 */
 } gpb_stats;
 
 /* intermediates available through gpb_fetch() (keep_intermediates = 1) */

@@ -81,3 +81,27 @@ def test_large_single_patch():
     assert np.isfinite(nm).all() and np.isfinite(orr).all() and nm.min() >= 0 and nm.max() > 0
     assert 0 < ctx.stats()["max_residual"] <= 4 * ctx.params.eig_tol
     ctx.close()
+
+
+def test_lanczos_fallback(orc):
+    """A block solver that misses its target (here: a matvec cap too small
+    for 32-vector filtering, ample for single-vector Lanczos) hands the batch
+    to plain Lanczos, and the result still matches the oracle."""
+    import gpb
+    from gpb import synth
+    img, cb = _img(64, 80, 6, 95)
+    ref = orc.globalpb(img, cb)
+    plain = gpb.Context(cb, eig_mode=gpb.EIG_LANCZOS)
+    plain.compute_batch([synth.pack_bgr(img)])
+    need = plain.stats()["matvecs_max"]
+    plain.close()
+    # enough for Lanczos, one fine outer iteration (32 + 43 x 32 matvecs) for the block solver
+    cap = max(1500, need + 50)
+    assert cap < 32 + 2 * 43 * 32
+    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM, eig_max_matvecs=cap)
+    nm, orr = ctx.compute_batch([synth.pack_bgr(img)])[0]
+    st = ctx.stats()
+    assert st["eig_fallback"] == 1 and ctx.last_status == gpb.GPB_OK
+    assert np.abs(nm - ref["nmax"]).max() < GPB_TOL
+    assert np.abs(orr.reshape(8, 64, 80) - ref["gpb_o"]).max() < GPB_TOL
+    ctx.close()

@@ -1303,6 +1303,12 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   } else {
     es = solve_lanczos(ctx, L);
   }
+  if (es == GPB_ERR_NOCONV && ctx->prm.eig_mode != GPB_EIG_LANCZOS) {
+    // the plain cold-start Lanczos solver is the fallback of the block
+    // solvers: the whole batch again, its own residual test and cap
+    ctx->stats.eig_fallback = 1;
+    es = solve_lanczos(ctx, L);
+  }
   if (es != GPB_OK && es != GPB_ERR_NOCONV) return es;
   if (ctx->prm.eig_mode != GPB_EIG_LANCZOS) {
     int berr = 0;
