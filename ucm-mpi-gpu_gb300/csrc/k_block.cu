@@ -181,24 +181,33 @@ __device__ __forceinline__ float f4get(const float4& v) {
 // that dominates near an eigenvector, where the diagonal and the
 // off-diagonal sum nearly cancel; used for the Rayleigh-Ritz products and
 // residuals, not the filter
+// a half-warp's sub-block: SB_R x SB_C pixels (the two halves of a warp
+// split its 4 x 4 block by rows), two block columns per lane
+constexpr int SB_R = 2, SB_C = 4, SB_N = SB_R * SB_C;
+
 template <class S, bool C, int RY, int DX, int I>
-__device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float v, float4 (&cw)[16], float (&acc)[16],
-                                            float (&lo)[16]) {
-  if constexpr (I < ST_B * ST_B) {
-    constexpr int bi = I / ST_B, bj = I % ST_B;
+__device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float2 v, float4 (&cw)[SB_N],
+                                            float2 (&acc)[SB_N], float2 (&lo)[SB_N]) {
+  if constexpr (I < SB_N) {
+    constexpr int bi = I / SB_C, bj = I % SB_C;
     if constexpr (S::in(RY - bi, DX - bj)) {
       constexpr int idx = S::index(RY - bi, DX - bj);
       // a pixel meets its offsets in scanline order, so chunk idx/4 is
       // first needed at idx % 4 == 0
       if constexpr (idx % 4 == 0) cw[I] = *(const float4*)(cs + (bi * ST_TX + bj) * S::NC + idx);
+      const float cf = f4get<idx % 4>(cw[I]);
       if constexpr (C) {
-        const float p = __fmul_rn(f4get<idx % 4>(cw[I]), v);
-        const float s = __fadd_rn(acc[I], p);
-        const float z = s - acc[I];
-        lo[I] += (acc[I] - (s - z)) + (p - z);
-        acc[I] = s;
+        float p = __fmul_rn(cf, v.x), s = __fadd_rn(acc[I].x, p), z = s - acc[I].x;
+        lo[I].x += (acc[I].x - (s - z)) + (p - z);
+        acc[I].x = s;
+        p = __fmul_rn(cf, v.y);
+        s = __fadd_rn(acc[I].y, p);
+        z = s - acc[I].y;
+        lo[I].y += (acc[I].y - (s - z)) + (p - z);
+        acc[I].y = s;
       } else {
-        acc[I] = fmaf(f4get<idx % 4>(cw[I]), v, acc[I]);
+        acc[I].x = fmaf(cf, v.x, acc[I].x);
+        acc[I].y = fmaf(cf, v.y, acc[I].y);
       }
     }
     step_pixels<S, C, RY, DX, I + 1>(cs, v, cw, acc, lo);
@@ -207,18 +216,18 @@ __device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float 
 
 template <class S, bool C, int P>
 __device__ __forceinline__ void step_positions(const float* __restrict__ ys, const float* __restrict__ cs,
-                                               float4 (&cw)[16], float (&acc)[16], float (&lo)[16]) {
-  constexpr int NX = ST_B + 2 * S::R;
-  if constexpr (P < NX * NX) {
+                                               float4 (&cw)[SB_N], float2 (&acc)[SB_N], float2 (&lo)[SB_N]) {
+  constexpr int NY = SB_R + 2 * S::R, NX = SB_C + 2 * S::R;
+  if constexpr (P < NY * NX) {
     constexpr int RY = P / NX - S::R, DX = P % NX - S::R;
     constexpr bool any = [] {
-      for (int i = 0; i < ST_B; i++)
-        for (int j = 0; j < ST_B; j++)
+      for (int i = 0; i < SB_R; i++)
+        for (int j = 0; j < SB_C; j++)
           if (S::in(RY - i, DX - j)) return true;
       return false;
     }();
     if constexpr (any) {
-      const float v = ys[((RY + S::R) * StepSmem<S>::PW + (DX + S::R)) * kBlk];
+      const float2 v = *(const float2*)(ys + ((RY + S::R) * StepSmem<S>::PW + (DX + S::R)) * kBlk);
       step_pixels<S, C, RY, DX, 0>(cs, v, cw, acc, lo);
     }
     step_positions<S, C, P + 1>(ys, cs, cw, acc, lo);
@@ -303,7 +312,10 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
     }
   }
   // ------------------------------------------------------------ consumers
-  const int by = (warp / (ST_TX / ST_B)) * ST_B, bx = (warp % (ST_TX / ST_B)) * ST_B;
+  // warp: a 4 x 4 block of the tile; half-warp h: its rows 2h, 2h+1; lane:
+  // block columns col, col + 1
+  const int by = (warp / (ST_TX / ST_B)) * ST_B + SB_R * (lane >> 4), bx = (warp % (ST_TX / ST_B)) * ST_B;
+  const int col = 2 * (lane & 15);
   for (int i = 0;; i++) {
     const int st = i & 1;
     if (!mbar_wait(full + st, (i >> 1) & 1)) {
@@ -314,32 +326,33 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
     if (m.end) return;
     const float* ys = (const float*)(smem + st * SM::stage);
     const float* cs = (const float*)(smem + st * SM::stage + SM::y_bytes);
-    // the previous iterate's values for this lane's column, fetched now so
+    // the previous iterate's values for this lane's columns, fetched now so
     // the loads overlap the stencil
-    float xr[16];
+    float2 xr[SB_N];
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-      const int y = m.y0 + by + k / ST_B, x = m.x0 + bx + k % ST_B;
-      xr[k] = (m.cz != 0.f && y < m.H && x < m.W) ? X[(m.vec + (long long)y * m.W + x) * kBlk + lane] : 0.f;
+    for (int k = 0; k < SB_N; k++) {
+      const int y = m.y0 + by + k / SB_C, x = m.x0 + bx + k % SB_C;
+      const bool ok = m.cz != 0.f && y < m.H && x < m.W;
+      xr[k] = ok ? *(const float2*)(X + (m.vec + (long long)y * m.W + x) * kBlk + col) : make_float2(0.f, 0.f);
     }
-    float acc[16], lo[16];
-    float4 cw[16];
+    float2 acc[SB_N], lo[SB_N];
+    float4 cw[SB_N];
 #pragma unroll
-    for (int k = 0; k < 16; k++) acc[k] = lo[k] = 0.f;
-    step_positions<S, C, 0>(ys + (by * SM::PW + bx) * kBlk + lane, cs + (by * ST_TX + bx) * S::NC, cw, acc, lo);
-    if constexpr (C) {
+    for (int k = 0; k < SB_N; k++) acc[k] = lo[k] = make_float2(0.f, 0.f);
+    step_positions<S, C, 0>(ys + (by * SM::PW + bx) * kBlk + col, cs + (by * ST_TX + bx) * S::NC, cw, acc, lo);
 #pragma unroll
-      for (int k = 0; k < 16; k++) acc[k] += lo[k];
-    }
-#pragma unroll
-    for (int k = 0; k < 16; k++) {
-      const int y = m.y0 + by + k / ST_B, x = m.x0 + bx + k % ST_B;
+    for (int k = 0; k < SB_N; k++) {
+      const int y = m.y0 + by + k / SB_C, x = m.x0 + bx + k % SB_C;
       if (y >= m.H || x >= m.W) continue;
       const long long q = m.vec + (long long)y * m.W + x;
-      const float yc = ys[((by + k / ST_B + S::R) * SM::PW + bx + k % ST_B + S::R) * kBlk + lane];
-      float r = m.cx * acc[k] + m.cy * yc;
-      if (m.cz != 0.f) r = fmaf(m.cz, xr[k], r);
-      out[q * kBlk + lane] = r;
+      const float2 yc = *(const float2*)(ys + ((by + k / SB_C + S::R) * SM::PW + bx + k % SB_C + S::R) * kBlk + col);
+      const float2 a0 = C ? make_float2(acc[k].x + lo[k].x, acc[k].y + lo[k].y) : acc[k];
+      float2 r = make_float2(m.cx * a0.x + m.cy * yc.x, m.cx * a0.y + m.cy * yc.y);
+      if (m.cz != 0.f) {
+        r.x = fmaf(m.cz, xr[k].x, r.x);
+        r.y = fmaf(m.cz, xr[k].y, r.y);
+      }
+      *(float2*)(out + q * kBlk + col) = r;
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(empty + st);
