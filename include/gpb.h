@@ -243,6 +243,59 @@ gpb_status gpb_write_png_minmax(const char* path, const float* data, uint32_t ro
 gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* d_packed,
                                     uint32_t* d_labels, void* stream);
 
+/* ---- Oriented watershed transform and ultrametric contour map ----------
+ * Contours2Ucm (src/contours2ucm.cpp:405-490, called from
+ * UCM_generator::generateUCM2, src/UCMgenerator.cpp:23-51), the consumer of
+ * GlobalPbCuda's orientation planes.
+ *
+ * orient      8 planes of width x height floats, row-major, plane o being
+ *             gPbOrient[o] as GlobalPbCuda returns it (after the sigmoid, in
+ *             oriMap order); device memory when orient_on_device, else host.
+ * double_size 1: ucm_out receives the (2H+1) x (2W+1) map of the doubled
+ *             grid ("doubleSize", what main.cpp:457 asks for); 0: the
+ *             (H+1) x (W+1) map of its even-even points.  Row-major doubles.
+ * The quantisation, flooding, painting, super-contour grid, cleaning and
+ * labelling run on the context's device; contour fitting and the greedy
+ * merge on the calling thread.  Not reentrant per context. */
+typedef struct {
+  uint32_t n_regions;   /* regions of the finest partition              */
+  uint32_t n_vertices;  /* vertices and edges of the fitted contours     */
+  uint32_t n_edges;
+  uint32_t n_artefacts; /* isolated zeros fixed by the cleaning step     */
+  int32_t fit_ok;       /* 0: the chords could not be made consistent;
+                           as in the reference nothing was painted      */
+  double ms_front;      /* device: max, quantise, flood                  */
+  double ms_fit;        /* host: contour fitting                         */
+  double ms_mid;        /* device: paint, super contour, clean, label    */
+  double ms_merge;      /* host: mean-boundary merge and calibration     */
+  double ms_total;
+} gpb_ucm_info;
+
+gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, const float* orient, int orient_on_device,
+                   int double_size, double* ucm_out, gpb_ucm_info* info);
+
+/* The host stages, usable without a device.
+ * gpb_ucm_fit_contours: fit_contour (src/fit_contour.cpp) of a 0/1 map of
+ *   watershed arcs, row-major height x width.  Vertices as (row, column)
+ *   pairs, edges as vertex-id pairs, each edge's interior pixels (row,
+ *   column) in off[e] .. off[e+1]; completion edges are not produced.
+ *   Returns the number of edges, -1 when a capacity is too small, -2 when
+ *   the chords cannot be made consistent (the reference then returns no
+ *   contours).
+ * gpb_ucm_mean_pb: UcmMeanPb (src/ucm_mean_pb.cpp:402-449): the
+ *   (2H+1) x (2W+1) mean-boundary map from ws_wt2 and the pixels' region
+ *   ids (0-based; negative ids are skipped), all row-major.
+ * gpb_ucm_labels_at_scale: UCM_generator::generateLabelsAtScaleK
+ *   (src/UCMgenerator.cpp:120-161): regions of the doubled-grid map at
+ *   threshold k, labels (0-based) of the height x width pixels; returns the
+ *   number of regions. */
+int32_t gpb_ucm_fit_contours(const uint8_t* bw, uint32_t width, uint32_t height, int32_t cap_vertices,
+                             int32_t cap_edges, int32_t cap_pixels, int32_t* n_vertices, int32_t* vertices,
+                             int32_t* edges, int32_t* off, int32_t* pixels);
+gpb_status gpb_ucm_mean_pb(const double* ws_wt2, const int32_t* labels, uint32_t width, uint32_t height,
+                           double* ucm);
+int32_t gpb_ucm_labels_at_scale(const double* ucm2, uint32_t width, uint32_t height, double k, int32_t* labels);
+
 int gpb_device_count(void);
 const char* gpb_status_str(gpb_status s);
 void gpb_free(void* p);

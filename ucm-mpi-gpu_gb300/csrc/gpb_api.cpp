@@ -212,6 +212,9 @@ struct gpb_ctx {
   uint64_t token = 0;          // identifies this context's constant tables
   Buf b;
   std::string last_error;
+  // device scratch of the OWT-UCM stage (ucm_api.cpp), freed with the context
+  void* ucm_state = nullptr;
+  void (*ucm_free)(void*) = nullptr;
   // last call
   std::vector<PatchDev> patches;
   long long total_pix = 0, lvec = 0;
@@ -438,6 +441,7 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
 extern "C" void gpb_destroy(gpb_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  if (ctx->ucm_free) ctx->ucm_free(ctx->ucm_state);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   {
     ConstBank& bk = bank_of(ctx->device);
@@ -1600,3 +1604,14 @@ extern "C" gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uin
     return GPB_ERR_CUDA;
   return GPB_OK;
 }
+
+// Accessors for the stages compiled in other translation units.
+namespace gpb {
+int ctx_device(gpb_ctx* c) { return c->device; }
+cudaStream_t ctx_stream(gpb_ctx* c) { return c->st; }
+void ctx_set_error(gpb_ctx* c, const char* m) { c->last_error = m; }
+void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*)) {
+  c->ucm_free = release;
+  return c->ucm_state;
+}
+}  // namespace gpb

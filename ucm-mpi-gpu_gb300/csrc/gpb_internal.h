@@ -6,6 +6,8 @@
 
 #include <vector>
 
+struct gpb_ctx;
+
 namespace gpb {
 
 constexpr int kNori = 8;
@@ -84,5 +86,11 @@ void oe_filter(double theta, double* out49);
 
 // kernel launchers (defined in the .cu files); all return cudaError_t of the launch
 struct DevTables;
+
+// context accessors for stages in other translation units (gpb_api.cpp)
+int ctx_device(gpb_ctx* c);
+cudaStream_t ctx_stream(gpb_ctx* c);
+void ctx_set_error(gpb_ctx* c, const char* m);
+void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*));
 
 }  // namespace gpb

@@ -1,0 +1,25 @@
+// ucm_host.h -- host stages of the oriented watershed transform and the
+// ultrametric contour map (ucm_host.cpp).
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#include <vector>
+
+namespace gpb {
+namespace ucm {
+
+struct FitResult {
+  std::vector<int32_t> vx, vy;    // vertex (row, column)
+  std::vector<int32_t> es, ee;    // edge start / end vertex
+  std::vector<int32_t> off, px;   // edge e's interior pixels (row * W + column) are px[off[e] .. off[e+1])
+};
+
+uint32_t components8(const uint8_t* bw, int H, int W, std::vector<uint32_t>& lab);
+bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out);
+int edge_orientation(int x1, int y1, int x2, int y2);
+void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm);
+void normalize(double* u, size_t n);
+
+}  // namespace ucm
+}  // namespace gpb
