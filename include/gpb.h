@@ -274,6 +274,15 @@ typedef struct {
 gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, const float* orient, int orient_on_device,
                    int double_size, double* ucm_out, gpb_ucm_info* info);
 
+/* Intermediates of the last gpb_ucm call on this context, copied to host:
+ * GPB_UCM_QUANT   u8, H x W: the 8-bit max-over-orientations image
+ * GPB_UCM_ARCS    u8, H x W: 1 on watershed pixels
+ * GPB_UCM_WSWT    float, H x W: contour strength painted along the edges
+ * GPB_UCM_WSWT2   float, (2H+1) x (2W+1): the cleaned doubled grid ws_wt2
+ * GPB_UCM_REGIONS int32, H x W: region ids of the finest partition */
+enum { GPB_UCM_QUANT = 0, GPB_UCM_ARCS = 1, GPB_UCM_WSWT = 2, GPB_UCM_WSWT2 = 3, GPB_UCM_REGIONS = 4 };
+gpb_status gpb_ucm_fetch(gpb_ctx* ctx, int what, void* host, size_t bytes);
+
 /* The host stages, usable without a device.
  * gpb_ucm_fit_contours: fit_contour (src/fit_contour.cpp) of a 0/1 map of
  *   watershed arcs, row-major height x width.  Vertices as (row, column)

@@ -1,0 +1,153 @@
+"""OWT-UCM stage on the CPU: the oracle restatement against the golden
+fixtures written by the reference's own UCM sources, the library's host
+stages (contour fitting, mean-boundary merge, labels at a scale) against
+the same fixtures, and -- where the reference is built on this machine --
+both against the reference on further seeded inputs."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import ucm_oracle as uo  # noqa: E402
+
+GOLD = os.path.join(ROOT, "tests", "golden", "ucm_cases.npz")
+CASES = ["rand40x50", "rand80x64", "gpb48x64", "tiny5x7", "flat32"]
+UCM_TOL = 1e-12  # calibration goes through exp(); numpy's and libm's may differ in the last bit
+
+
+@pytest.fixture(scope="module")
+def gold():
+    z = np.load(GOLD)
+    return {c: {k.split("/", 1)[1]: z[k] for k in z.files if k.startswith(c + "/")} for c in CASES}
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_chain_matches_reference_fixtures(gold, case):
+    g = gold[case]
+    planes = g["planes"].astype(np.float64)
+    q = uo.quantize(planes)
+    assert np.array_equal(q, g["quant"])
+    assert np.array_equal((uo.watershed(q) == 0).astype(np.uint8), g["arcs"])
+    w = uo.paint(planes, g["vertices"], g["edges"], g["off"], g["pixels"])
+    assert np.array_equal(w, g["wswt"])
+    w2, lab, _, _ = uo.super_clean(w)
+    assert np.array_equal(w2, g["wswt2"]) and np.array_equal(lab, g["labels"])
+    u2 = uo.normalize(uo.mean_pb(w2, lab))
+    assert np.abs(u2 - g["ucm2"]).max() <= UCM_TOL
+    assert np.abs(uo.downsample(u2) - g["ucm"]).max() <= UCM_TOL
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_library_host_fit_matches_reference(gold, case):
+    import gpb
+    g = gold[case]
+    fit = gpb.ucm_fit_contours(g["arcs"])
+    assert fit is not None
+    vert, edges, off, px = fit
+    assert np.array_equal(vert, g["vertices"])
+    assert np.array_equal(edges, g["edges"])
+    assert np.array_equal(off, g["off"]) and np.array_equal(px, g["pixels"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_library_host_merge_matches_reference(gold, case):
+    import gpb
+    g = gold[case]
+    u = gpb.ucm_mean_pb(g["wswt2"], g["labels"])
+    assert np.array_equal(u, uo.mean_pb(g["wswt2"], g["labels"].astype(np.int64)))
+    assert np.abs(uo.normalize(u) - g["ucm2"]).max() <= UCM_TOL
+
+
+@pytest.mark.parametrize("k", [0.05, 0.2, 0.5])
+def test_labels_at_scale(gold, k):
+    import gpb
+    u2 = gold["rand80x64"]["ucm2"]
+    lab, n = gpb.ucm_labels_at_scale(u2, k)
+    ref_lab, ref_n = uo.labels_at_scale(u2, k)
+    assert n == ref_n and np.array_equal(lab, ref_lab)
+
+
+def test_fit_of_empty_map():
+    import gpb
+    vert, edges, off, px = gpb.ucm_fit_contours(np.zeros((9, 11), np.uint8))
+    assert len(vert) == 0 and len(edges) == 0 and list(off) == [0] and len(px) == 0
+
+
+# ---------------------------------------------------------------- against the reference itself
+
+def _planes(H, W, seed, sigma):
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    g = np.stack([gaussian_filter(rng.random((H, W)), sigma) for _ in range(8)])
+    g = (g - g.min()) / (g.max() - g.min())
+    return np.ascontiguousarray((g ** 2).astype(np.float32).astype(np.float64))
+
+
+def _P(a):
+    import ctypes
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _ref_fit(L, bw):
+    H, W = bw.shape
+    cv, ce, cp = H * W, 4 * H * W, 4 * H * W
+    nv = np.zeros(1, np.int32)
+    vert, ed = np.zeros(2 * cv, np.int32), np.zeros(2 * ce, np.int32)
+    cm, off, xy = np.zeros(ce, np.int32), np.zeros(ce + 1, np.int32), np.zeros(2 * cp, np.int32)
+    ne = L.ref_ucm_fit_contour(_P(np.ascontiguousarray(bw, np.float64)), H, W, cv, ce, cp, _P(nv), _P(vert),
+                               _P(ed), _P(cm), _P(off), _P(xy))
+    nc = int((cm[:ne] == 0).sum())
+    return vert[:2 * nv[0]].reshape(-1, 2), ed[:2 * nc].reshape(-1, 2), off[:nc + 1], xy[:2 * off[nc]].reshape(-1, 2)
+
+
+@pytest.mark.parametrize("H,W,seed,sigma", [(64, 64, 2, 2.0), (128, 160, 4, 2.5), (200, 200, 5, 1.8),
+                                            (266, 266, 6, 2.0), (150, 90, 8, 1.0)])
+def test_host_stages_against_reference(ref, H, W, seed, sigma):
+    import gpb
+    L = ref.ref()
+    g = _planes(H, W, seed, sigma)
+    q = uo.quantize(g)
+    ws = np.zeros((H, W), np.int32)
+    L.ref_ucm_watershed(_P(q), H, W, _P(ws))
+    bw = (ws == 0).astype(np.uint8)
+    mine, theirs = gpb.ucm_fit_contours(bw), _ref_fit(L, bw)
+    for a, b in zip(mine, theirs):
+        assert np.array_equal(a, b)
+    w = np.zeros((H, W))
+    L.ref_ucm_finest_partition(_P(g), H, W, _P(w))
+    w2, lab = np.zeros((2 * H + 1, 2 * W + 1)), np.zeros((H, W), np.int32)
+    L.ref_ucm_super_clean(_P(w), H, W, _P(w2), _P(lab))
+    u = np.zeros_like(w2)
+    L.ref_ucm_mean_pb(_P(w2), _P(lab), H, W, _P(u))
+    assert np.array_equal(gpb.ucm_mean_pb(w2, lab), u)
+
+
+@pytest.mark.parametrize("H,W,seed,sigma", [(40, 50, 1, 1.5), (64, 64, 2, 2.0), (90, 70, 9, 1.1)])
+def test_oracle_pins_against_reference(ref, H, W, seed, sigma):
+    L = ref.ref()
+    g = _planes(H, W, seed, sigma)
+    q = uo.quantize(g)
+    ws = np.zeros((H, W), np.int32)
+    L.ref_ucm_watershed(_P(q), H, W, _P(ws))
+    assert np.array_equal(uo.watershed(q) == 0, ws == 0)
+    vert, edges, off, px = _ref_fit(L, (ws == 0).astype(np.uint8))
+    w = np.zeros((H, W))
+    L.ref_ucm_finest_partition(_P(g), H, W, _P(w))
+    assert np.array_equal(uo.paint(g, vert, edges, off, px), w)
+    w2, lab = np.zeros((2 * H + 1, 2 * W + 1)), np.zeros((H, W), np.int32)
+    L.ref_ucm_super_clean(_P(w), H, W, _P(w2), _P(lab))
+    ow2, olab, _, _ = uo.super_clean(w)
+    assert np.array_equal(ow2, w2) and np.array_equal(olab, lab)
+    u = np.zeros_like(w2)
+    L.ref_ucm_mean_pb(_P(w2), _P(lab), H, W, _P(u))
+    assert np.array_equal(uo.mean_pb(w2, lab.astype(np.int64)), u)
+    full = np.zeros_like(w2)
+    L.ref_ucm_contours2ucm(_P(g), H, W, 1, _P(full))
+    assert np.abs(uo.normalize(u) - full).max() <= UCM_TOL
+    bwl = (w2[:-1, :-1] == 0).astype(np.int32)
+    rl = np.zeros_like(bwl)
+    L.ref_ucm_bwlabel(_P(np.ascontiguousarray(bwl)), bwl.shape[0], bwl.shape[1], _P(rl))
+    assert np.array_equal(uo.bwlabel(bwl == 1)[0], rl)

@@ -24,6 +24,7 @@ struct UcmState {
   size_t cap_paint = 0;    // entries of the paint list
   float* orient = nullptr; // staging of host planes
   size_t cap_orient = 0;
+  int H = 0, W = 0;        // the last call's image
 };
 
 void ucm_release(void* p) {
@@ -95,6 +96,8 @@ extern "C" gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, con
   if (!slot) slot = new UcmState();
   UcmState& u = *(UcmState*)slot;
   UCK(ucm_reserve(u, H, W));
+  u.H = 0;
+  u.W = 0;
   const float* d_orient = orient;
   if (!orient_on_device) {
     if (u.cap_orient < 8 * N) {
@@ -174,6 +177,8 @@ extern "C" gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, con
       for (int j = 0; j <= W; j++)
         ucm_out[(size_t)i * (W + 1) + j] = (i < H && j < W) ? um[(size_t)(2 * i + 2) * GW + 2 * j + 2] : 0.0;
   }
+  u.H = H;
+  u.W = W;
   if (info) {
     info->n_regions = (uint32_t)counts[0];
     info->n_vertices = (uint32_t)fit.vx.size();
@@ -234,4 +239,27 @@ extern "C" int32_t gpb_ucm_labels_at_scale(const double* ucm2, uint32_t width, u
     for (uint32_t j = 0; j < width; j++)
       labels[(size_t)i * width + j] = (int32_t)l2[(size_t)(2 * i + 1) * GW + 2 * j + 1] - 1;
   return (int32_t)n;
+}
+
+extern "C" gpb_status gpb_ucm_fetch(gpb_ctx* ctx, int what, void* host, size_t bytes) {
+  if (!ctx || !host) return GPB_ERR_ARG;
+  void*& slot = ctx_ucm_state(ctx, ucm_release);
+  UcmState* u = (UcmState*)slot;
+  if (!u || !u->H) return GPB_ERR_ARG;
+  const size_t N = (size_t)u->H * u->W, N2 = (size_t)(2 * u->H + 1) * (2 * u->W + 1);
+  const void* src = nullptr;
+  size_t need = 0;
+  switch (what) {
+    case GPB_UCM_QUANT: src = u->s.q; need = N; break;
+    case GPB_UCM_ARCS: src = u->s.bw; need = N; break;
+    case GPB_UCM_WSWT: src = u->s.wswt; need = N * sizeof(float); break;
+    case GPB_UCM_WSWT2: src = u->s.wswt2; need = N2 * sizeof(float); break;
+    case GPB_UCM_REGIONS: src = u->s.labels; need = N * sizeof(int32_t); break;
+    default: return GPB_ERR_ARG;
+  }
+  if (bytes < need) return GPB_ERR_ARG;
+  UCK(cudaSetDevice(ctx_device(ctx)));
+  UCK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, ctx_stream(ctx)));
+  UCK(cudaStreamSynchronize(ctx_stream(ctx)));
+  return GPB_OK;
 }

@@ -21,6 +21,7 @@ LIBPATH = os.path.join(_HERE, "libgpb.so")
  GPB_ERR_TOO_LARGE) = range(8)
 STATIC_MAX_PIXELS = 1 << 20   # gpb_texton_labels_static's scratch limit
 STITCH_LAST, STITCH_INTERIOR, STITCH_BLEND = 0, 1, 2
+UCM_QUANT, UCM_ARCS, UCM_WSWT, UCM_WSWT2, UCM_REGIONS = range(5)
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
 EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
@@ -49,6 +50,16 @@ class Patch(ctypes.Structure):
 
 class Result(ctypes.Structure):
     _fields_ = [("nmax", ctypes.c_void_p), ("orient", ctypes.c_void_p)]
+
+
+class UcmInfo(ctypes.Structure):
+    _fields_ = [("n_regions", ctypes.c_uint32), ("n_vertices", ctypes.c_uint32), ("n_edges", ctypes.c_uint32),
+                ("n_artefacts", ctypes.c_uint32), ("fit_ok", ctypes.c_int32), ("ms_front", ctypes.c_double),
+                ("ms_fit", ctypes.c_double), ("ms_mid", ctypes.c_double), ("ms_merge", ctypes.c_double),
+                ("ms_total", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Stats(ctypes.Structure):
@@ -108,6 +119,17 @@ def _lib():
         L.gpb_superpixel_features.restype = c
         L.gpb_texton_labels_static.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
         L.gpb_texton_labels_static.restype = c
+        u32, i32 = ctypes.c_uint32, ctypes.c_int32
+        L.gpb_ucm.argtypes = [vp, u32, u32, vp, c, c, vp, ctypes.POINTER(UcmInfo)]
+        L.gpb_ucm.restype = c
+        L.gpb_ucm_fetch.argtypes = [vp, c, vp, sz]
+        L.gpb_ucm_fetch.restype = c
+        L.gpb_ucm_fit_contours.argtypes = [vp, u32, u32, i32, i32, i32, vp, vp, vp, vp, vp]
+        L.gpb_ucm_fit_contours.restype = i32
+        L.gpb_ucm_mean_pb.argtypes = [vp, vp, u32, u32, vp]
+        L.gpb_ucm_mean_pb.restype = c
+        L.gpb_ucm_labels_at_scale.argtypes = [vp, u32, u32, ctypes.c_double, vp]
+        L.gpb_ucm_labels_at_scale.restype = i32
         _L = L
     return _L
 
@@ -219,10 +241,81 @@ class Context:
         _check(_lib().gpb_texton_labels_static(self._h, width, height, d_packed, d_labels, stream),
                "gpb_texton_labels_static")
 
+    def ucm(self, orient, double_size=True, d_orient=None, shape=None):
+        """Contours2Ucm of 8 orientation planes: ``orient`` an (8, H, W) host
+        array, or ``d_orient`` a device pointer with ``shape`` = (H, W).
+        Returns the map (float64, (2H+1, 2W+1) or (H+1, W+1)) and the info
+        dict of the call."""
+        if d_orient is None:
+            a = np.ascontiguousarray(orient, np.float32)
+            if a.ndim != 3 or a.shape[0] != 8:
+                raise ValueError("orient must be 8 x H x W")
+            H, W = a.shape[1:]
+            ptr, on_dev = a.ctypes.data, 0
+        else:
+            H, W = shape
+            ptr, on_dev = d_orient, 1
+        out = np.empty((2 * H + 1, 2 * W + 1) if double_size else (H + 1, W + 1), np.float64)
+        info = UcmInfo()
+        _check(_lib().gpb_ucm(self._h, W, H, ptr, on_dev, 1 if double_size else 0, out.ctypes.data,
+                              ctypes.byref(info)), "gpb_ucm")
+        self.last_ucm_shape = (H, W)
+        return out, info.as_dict()
+
+    def ucm_fetch(self, what):
+        """an intermediate of the last ucm call (UCM_* names)"""
+        H, W = self.last_ucm_shape
+        shape, dt = {UCM_QUANT: ((H, W), np.uint8), UCM_ARCS: ((H, W), np.uint8), UCM_WSWT: ((H, W), np.float32),
+                     UCM_WSWT2: ((2 * H + 1, 2 * W + 1), np.float32), UCM_REGIONS: ((H, W), np.int32)}[what]
+        out = np.empty(shape, dt)
+        _check(_lib().gpb_ucm_fetch(self._h, what, out.ctypes.data, out.nbytes), "gpb_ucm_fetch")
+        return out
+
     def stats(self):
         s = Stats()
         _check(_lib().gpb_last_stats(self._h, ctypes.byref(s)), "gpb_last_stats")
         return s.as_dict()
+
+
+def ucm_fit_contours(bw):
+    """fit_contour of a 0/1 watershed-arc map on the host: (vertices (V, 2),
+    edges (E, 2), off (E+1,), pixels (P, 2)), or None where the chords
+    cannot be made consistent."""
+    b = np.ascontiguousarray(bw, np.uint8)
+    H, W = b.shape
+    cv, ce, cp = H * W, 4 * H * W, 4 * H * W
+    nv = np.zeros(1, np.int32)
+    vert = np.zeros(2 * cv, np.int32)
+    ed = np.zeros(2 * ce, np.int32)
+    off = np.zeros(ce + 1, np.int32)
+    px = np.zeros(2 * cp, np.int32)
+    ne = _lib().gpb_ucm_fit_contours(b.ctypes.data, W, H, cv, ce, cp, nv.ctypes.data, vert.ctypes.data,
+                                     ed.ctypes.data, off.ctypes.data, px.ctypes.data)
+    if ne == -2:
+        return None
+    if ne < 0:
+        raise GpbError(GPB_ERR_ARG, "gpb_ucm_fit_contours")
+    return (vert[:2 * nv[0]].reshape(-1, 2), ed[:2 * ne].reshape(-1, 2), off[:ne + 1],
+            px[:2 * off[ne]].reshape(-1, 2))
+
+
+def ucm_mean_pb(ws_wt2, labels):
+    """UcmMeanPb on the host: the (2H+1, 2W+1) map before calibration."""
+    w = np.ascontiguousarray(ws_wt2, np.float64)
+    lab = np.ascontiguousarray(labels, np.int32)
+    H, W = lab.shape
+    out = np.empty((2 * H + 1, 2 * W + 1), np.float64)
+    _check(_lib().gpb_ucm_mean_pb(w.ctypes.data, lab.ctypes.data, W, H, out.ctypes.data), "gpb_ucm_mean_pb")
+    return out
+
+
+def ucm_labels_at_scale(ucm2, k):
+    """generateLabelsAtScaleK: (labels H x W, number of regions)."""
+    u = np.ascontiguousarray(ucm2, np.float64)
+    H, W = (u.shape[0] - 1) // 2, (u.shape[1] - 1) // 2
+    lab = np.empty((H, W), np.int32)
+    n = _lib().gpb_ucm_labels_at_scale(u.ctypes.data, W, H, float(k), lab.ctypes.data)
+    return lab, n
 
 
 def write_piece_files(prefix, nmax, orient):
