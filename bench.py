@@ -244,6 +244,29 @@ def run_gpu(args):
     pctx.close()
     peak, peak_kind = peaks()
     kname, kms, kn, kb = "cf_step", ps["spmv_ms"], ps["spmv_launches"], ps["spmv_bytes"]
+    # the consumer of the step's output: OWT-UCM of the stitched 1024 x 1024
+    # orientation planes (wall time of gpb_ucm, device planes in, host map out)
+    ucm = None
+    if not args.no_ucm:
+        places = [(x0, y0, ix, iy, iw, ih) for (y0, x0, h, w, iy, ix, ih, iw) in boxes]
+        d_snm = torch.empty(1024 * 1024, dtype=torch.float32, device="cuda")
+        d_sor = torch.empty(8 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        dev_step()
+        ctx.stitch_device(gpb.STITCH_INTERIOR, 1024, 1024, places, d_snm.data_ptr(), d_sor.data_ptr())
+        torch.cuda.synchronize()
+        ctx.ucm(None, d_orient=d_sor.data_ptr(), shape=(1024, 1024))
+        uts, info = [], None
+        for _ in range(args.ucm_steps):
+            t0 = time.perf_counter()
+            _, info = ctx.ucm(None, d_orient=d_sor.data_ptr(), shape=(1024, 1024))
+            uts.append((time.perf_counter() - t0) * 1e3)
+        ums = float(np.mean(uts))
+        ucm = {"image": "the step's 1024 x 1024 stitched gPb orientation planes", "ms": ums,
+               "mpix_s": 1024 * 1024 / 1e6 / (ums / 1e3), "steps": args.ucm_steps,
+               "stages_ms": {k: info[k] for k in ("ms_front", "ms_fit", "ms_mid", "ms_merge")},
+               "regions": info["n_regions"], "edges": info["n_edges"], "artefacts": info["n_artefacts"]}
+        if args.ucm_save:
+            np.save(args.ucm_save, d_sor.cpu().numpy().reshape(8, 1024, 1024))
     achieved = (kb / kn) / (kms / kn / 1e3) / 1e9 if kn else None
     last = st_acc[-1]
     if rank == 0:
@@ -271,6 +294,7 @@ def run_gpu(args):
             "eig": {"matvecs_max": last["matvecs_max"], "restarts": last["restarts"],
                     "max_residual": last["max_residual"]},
             "texton_repaired": last["texton_repaired"],
+            "ucm": ucm,
         }
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(img, cb, boxes, seconds=args.cpu_seconds)
@@ -290,6 +314,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-ucm", action="store_true")
+    ap.add_argument("--ucm-steps", type=int, default=3)
+    ap.add_argument("--ucm-save", default=None, help="write the UCM input planes (.npy) to this path")
     ap.add_argument("--ncu-case", action="store_true", help="one batch only (for ncu captures)")
     ap.add_argument("--ncu-eig", default="warm", choices=["warm", "block"])
     args = ap.parse_args()
