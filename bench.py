@@ -255,10 +255,10 @@ def run_gpu(args):
         ctx.stitch_device(gpb.STITCH_INTERIOR, 1024, 1024, places, d_snm.data_ptr(), d_sor.data_ptr())
         torch.cuda.synchronize()
         ctx.ucm(None, d_orient=d_sor.data_ptr(), shape=(1024, 1024))
-        uts, info = [], None
+        uts, info, umap = [], None, None
         for _ in range(args.ucm_steps):
             t0 = time.perf_counter()
-            _, info = ctx.ucm(None, d_orient=d_sor.data_ptr(), shape=(1024, 1024))
+            umap, info = ctx.ucm(None, d_orient=d_sor.data_ptr(), shape=(1024, 1024))
             uts.append((time.perf_counter() - t0) * 1e3)
         ums = float(np.mean(uts))
         ucm = {"image": "the step's 1024 x 1024 stitched gPb orientation planes", "ms": ums,
@@ -267,6 +267,8 @@ def run_gpu(args):
                "regions": info["n_regions"], "edges": info["n_edges"], "artefacts": info["n_artefacts"]}
         if args.ucm_save:
             np.save(args.ucm_save, d_sor.cpu().numpy().reshape(8, 1024, 1024))
+            np.save(args.ucm_save[:-4] + "_map.npy" if args.ucm_save.endswith(".npy") else args.ucm_save + "_map",
+                    umap)
     achieved = (kb / kn) / (kms / kn / 1e3) / 1e9 if kn else None
     last = st_acc[-1]
     if rank == 0:
@@ -316,7 +318,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-ucm", action="store_true")
     ap.add_argument("--ucm-steps", type=int, default=3)
-    ap.add_argument("--ucm-save", default=None, help="write the UCM input planes (.npy) to this path")
+    ap.add_argument("--ucm-save", default=None, help="write the UCM input planes (.npy) to this path and the map beside it")
     ap.add_argument("--ncu-case", action="store_true", help="one batch only (for ncu captures)")
     ap.add_argument("--ncu-eig", default="warm", choices=["warm", "block"])
     args = ap.parse_args()

@@ -136,13 +136,18 @@ __global__ void __launch_bounds__(32) k_ws_rowsort(const uint8_t* __restrict__ q
   }
 }
 
-// One CTA of 256 threads per image, thread l owning grey level l.  ws is
-// -1 (not reached), 0 (watershed pixel) or a region label (> 0): a new
-// region takes the label 1 + its pixel index.
-__global__ void __launch_bounds__(256) k_ws_flood(const UcmImage* __restrict__ imgs, const int32_t* __restrict__ off,
-                                                  const uint16_t* __restrict__ cols, int32_t* __restrict__ ws) {
+// One CTA of 1024 threads per image; warp w owns grey levels w, w + 32, ...
+// At step t a warp takes, level by level, the row t - 2l of its level l
+// and walks that row's pixels of level l in column order, 32 at a time:
+// every lane gathers the labels of its pixel's 8 neighbours at once (the
+// pixel to its left is still unlabelled when it is the previous lane's,
+// so it is left out), then runs of adjacent pixels are resolved lane by
+// lane.  ws is -1 (not reached), 0 (watershed pixel) or a region label
+// (> 0): a new region takes the label 1 + its pixel index.
+__global__ void __launch_bounds__(1024) k_ws_flood(const UcmImage* __restrict__ imgs, const int32_t* __restrict__ off,
+                                                   const uint16_t* __restrict__ cols, int32_t* __restrict__ ws) {
   const UcmImage I = imgs[blockIdx.x];
-  const int H = I.H, W = I.W, lvl = threadIdx.x;
+  const int H = I.H, W = I.W, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int32_t* L = ws + I.pix;
   const int32_t* O = off + I.row0 * 257;
   const uint16_t* C = cols + I.pix;
@@ -150,23 +155,45 @@ __global__ void __launch_bounds__(256) k_ws_flood(const UcmImage* __restrict__ i
   __syncthreads();
   const int steps = 2 * 255 + H;
   for (int t = 0; t < steps; t++) {
-    const int x = t - 2 * lvl;
-    if (x >= 0 && x < H) {
+    for (int lvl = warp; lvl < 256; lvl += 32) {
+      const int x = t - 2 * lvl;
+      if (x < 0 || x >= H) continue;
       const int b = O[x * 257 + lvl], e = O[x * 257 + lvl + 1];
-      for (int k = b; k < e; k++) {
-        const int y = C[(size_t)x * W + k];
-        int state = -1;
-        for (int i = -1; i <= 1; i++) {
-          const int xi = x + i;
-          if (xi < 0 || xi >= H) continue;
-          for (int j = -1; j <= 1; j++) {
-            const int yj = y + j;
-            if ((i == 0 && j == 0) || yj < 0 || yj >= W) continue;
-            const int v = L[(size_t)xi * W + yj];
-            if (v > 0) state = (state == -1) ? v : (v != state ? 0 : state);
+      for (int k0 = b; k0 < e; k0 += 32) {
+        const int k = k0 + lane;
+        const bool in = k < e;
+        const int y = in ? C[(size_t)x * W + k] : -4;
+        const int yl = __shfl_up_sync(0xffffffffu, y, 1);
+        const bool dep = in && lane > 0 && yl == y - 1;  // its left neighbour is the previous lane's pixel
+        int s = -1;  // -1: no labelled neighbour, 0: two different labels, else the one label
+        if (in) {
+          for (int i = -1; i <= 1; i++) {
+            const int xi = x + i;
+            if (xi < 0 || xi >= H) continue;
+            for (int j = -1; j <= 1; j++) {
+              const int yj = y + j;
+              if ((i == 0 && j == 0) || yj < 0 || yj >= W) continue;
+              const int v = L[(size_t)xi * W + yj];
+              if (v > 0) s = (s == -1) ? v : (v != s ? 0 : s);
+            }
           }
         }
-        L[(size_t)x * W + y] = state >= 0 ? state : x * W + y + 1;
+        const int sl = __shfl_up_sync(0xffffffffu, s, 1);
+        const int mine = x * W + y + 1;
+        // final without the left lane: no dependence, a conflict already, or
+        // a label the left pixel can only repeat or have lost to a conflict
+        int done = !in || !dep || s == 0 || (s > 0 && (sl == s || sl == 0));
+        int val = !dep ? (s >= 0 ? s : mine) : s;
+        while (!__all_sync(0xffffffffu, done)) {
+          const int pv = __shfl_up_sync(0xffffffffu, val, 1);
+          const int pd = __shfl_up_sync(0xffffffffu, done, 1);
+          if (!done && pd) {
+            val = (s == -1) ? (pv > 0 ? pv : mine) : ((pv > 0 && pv != s) ? 0 : s);
+            done = 1;
+          }
+        }
+        if (in) L[(size_t)x * W + y] = val;
+        __syncwarp();
       }
     }
     __syncthreads();
@@ -440,7 +467,7 @@ cudaError_t ucm_front(const float* d_orient, int H, int W, UcmScratch& s, cudaSt
   k_ucm_pbmax<<<grid_for(N), 256, 0, st>>>(d_orient, N, s.pb, s.mm);
   k_ucm_quant<<<grid_for(N), 256, 0, st>>>(s.pb, N, s.mm, s.q);
   k_ws_rowsort<<<H, 32, 0, st>>>(s.q, H, W, s.off, s.cols);
-  k_ws_flood<<<1, 256, 0, st>>>(s.img, s.off, s.cols, s.ws);
+  k_ws_flood<<<1, 1024, 0, st>>>(s.img, s.off, s.cols, s.ws);
   k_ws_bw<<<grid_for(N), 256, 0, st>>>(s.ws, N, s.bw);
   return cudaGetLastError();
 }

@@ -251,7 +251,10 @@ void Contours::build(const uint8_t* bw) {
   std::vector<int> remap(vert.size(), -1);
   std::vector<Vert> kept;
   for (size_t v = 0; v < vert.size(); v++) {
-    if (vert[v].degree == 0) continue;
+    if (vert[v].degree == 0) {
+      is_v_[(size_t)vert[v].x * W_ + vert[v].y] = 0;
+      continue;
+    }
     remap[v] = (int)kept.size();
     kept.push_back(vert[v]);
   }
@@ -318,6 +321,7 @@ void Contours::split(int e_id, size_t p) {
   const int32_t at = edge[e_id].px[p];
   const int v = (int)vert.size();
   vert.push_back({(int)(at / W_), (int)(at % W_), 2});
+  is_v_[at] = 1;
   Edge tail;
   tail.vs = v;
   tail.ve = edge[e_id].ve;
@@ -500,11 +504,21 @@ bool Contours::subdivide_global() {
     // (b) two chords crossing at a point that is no vertex: the one whose
     // contour comes nearer the other's chord is kept, the other split
     std::vector<std::pair<int, int>> pairs;
-    for (const std::vector<int>& c : cell)
-      for (size_t i = 0; i < c.size(); i++)
-        for (size_t j = i + 1; j < c.size(); j++) pairs.push_back({std::min(c[i], c[j]), std::max(c[i], c[j])});
-    std::sort(pairs.begin(), pairs.end());
-    pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+    for (int cx = 0; cx < GX; cx++)
+      for (int cy = 0; cy < GY; cy++) {
+        const std::vector<int>& c = cell[(size_t)cx * GY + cy];
+        for (size_t i = 0; i < c.size(); i++)
+          for (size_t j = i + 1; j < c.size(); j++) {
+            const Vert &a0 = vert[edge[c[i]].vs], &a1 = vert[edge[c[i]].ve];
+            const Vert &b0 = vert[edge[c[j]].vs], &b1 = vert[edge[c[j]].ve];
+            const int lx = std::max(std::min(a0.x, a1.x), std::min(b0.x, b1.x));
+            const int ly = std::max(std::min(a0.y, a1.y), std::min(b0.y, b1.y));
+            const int hx = std::min(std::max(a0.x, a1.x), std::max(b0.x, b1.x));
+            const int hy = std::min(std::max(a0.y, a1.y), std::max(b0.y, b1.y));
+            if (lx > hx || ly > hy || lx / CS != cx || ly / CS != cy) continue;  // no overlap, or not its first cell
+            pairs.push_back({std::min(c[i], c[j]), std::max(c[i], c[j])});
+          }
+      }
     for (const auto& pr : pairs) {
       const int s = pr.first, t = pr.second;
       const i64 ax = vert[edge[s].vs].x, ay = vert[edge[s].vs].y, bx = vert[edge[s].ve].x, by = vert[edge[s].ve].y;
@@ -518,9 +532,7 @@ bool Contours::subdivide_global() {
       const i64 X = ax * den + (bx - ax) * num, Y = ay * den + (by - ay) * num;
       if (X % den == 0 && Y % den == 0) {  // an integer crossing point: is it a vertex?
         const i64 xi = X / den, yi = Y / den;
-        bool at_vertex = false;
-        for (size_t v = 0; v < nv && !at_vertex; v++) at_vertex = (vert[v].x == xi && vert[v].y == yi);
-        if (at_vertex) continue;  // handled under (a)
+        if (xi >= 0 && xi < H_ && yi >= 0 && yi < W_ && is_v_[(size_t)xi * W_ + yi]) continue;  // handled under (a)
       }
       found = true;
       // order the two as the sweep does at the crossing: by the angle of
@@ -616,14 +628,58 @@ int edge_orientation(int x1, int y1, int x2, int y2) {
 
 namespace {
 
-struct Nb {
+// One adjacent pair of regions, shared by both sides (the reference keeps a
+// copy in each region's neighbour map; both copies are always updated together).
+struct Pair {
   double energy = 0, total = 0, length = 0;
+  double pushed = -1.0;  // energy and first region of the pair's last queue entry
+  int first = -1;
+  int list = -1;         // the pair's boundary coordinates
 };
 
-struct Region {
-  std::vector<int> elements;                       // component ids
-  std::vector<std::pair<int, int>> boundary;       // (coord, neighbouring component)
-  std::map<int, Nb> nbr;
+// open-addressing map from an unordered region pair to its Pair index
+class PairTable {
+ public:
+  explicit PairTable(size_t expect) {
+    size_t c = 16;
+    while (c < 2 * expect) c <<= 1;
+    key_.assign(c, kEmpty);
+    val_.assign(c, -1);
+  }
+  // index of pair {a, b}, or -1; with create, a new pair is appended to `pairs`
+  int find(int a, int b, std::vector<Pair>* pairs) {
+    const uint64_t k = a < b ? ((uint64_t)(uint32_t)a << 32) | (uint32_t)b : ((uint64_t)(uint32_t)b << 32) | (uint32_t)a;
+    size_t h = (size_t)((k * 0x9E3779B97F4A7C15ull) >> 20) & (key_.size() - 1);
+    for (;; h = (h + 1) & (key_.size() - 1)) {
+      if (key_[h] == k) return val_[h];
+      if (key_[h] == kEmpty) break;
+    }
+    if (!pairs) return -1;
+    key_[h] = k;
+    val_[h] = (int)pairs->size();
+    pairs->emplace_back();
+    if (++used_ * 2 > key_.size()) grow();
+    return (int)pairs->size() - 1;
+  }
+
+ private:
+  static constexpr uint64_t kEmpty = ~0ull;
+  std::vector<uint64_t> key_;
+  std::vector<int> val_;
+  size_t used_ = 0;
+  void grow() {
+    std::vector<uint64_t> k2(key_.size() * 2, kEmpty);
+    std::vector<int> v2(key_.size() * 2, -1);
+    for (size_t i = 0; i < key_.size(); i++) {
+      if (key_[i] == kEmpty) continue;
+      size_t h = (size_t)((key_[i] * 0x9E3779B97F4A7C15ull) >> 20) & (k2.size() - 1);
+      while (k2[h] != kEmpty) h = (h + 1) & (k2.size() - 1);
+      k2[h] = key_[i];
+      v2[h] = val_[i];
+    }
+    key_.swap(k2);
+    val_.swap(v2);
+  }
 };
 
 struct Entry {
@@ -641,106 +697,157 @@ struct Entry {
 // ComputeUcm + CompleteContourMap (ucm_mean_pb.cpp:230-398) on the
 // (2H+1) x (2W+1) grid, row-major here (the reference stores it
 // column-major; the grid coordinates are the same).  lb: local boundary
-// strengths; part: H x W region ids 0..n-1.
+// strengths; part: H x W region ids 0..n-1 (negative ids are skipped).
+//
+// The reference sums each pair's boundary strengths in column-major order
+// of the coordinates; each pair's list is sorted into that order first.
+//
+// The reference walks the son's whole boundary on every merge, raising the
+// map to the merge's saliency.  Here each pair of regions keeps one list of
+// its boundary coordinates with a pending raise: the son-father list takes
+// the saliency when it closes, the son's other lists take it as a pending
+// raise and are joined to the father's (the shorter list, raised, into the
+// longer).  With saliencies that never decrease -- the reference stops
+// being defined otherwise: it frees its arrays and carries on -- every
+// coordinate ends at the saliency of the merge that joins its two sides,
+// as there.
+//
+// After every merge the reference pushes (d, k, father) for each neighbour
+// k of the father.  A push identical to the pair's last entry still in the
+// queue changes nothing (the copy pops right after it and fails the energy
+// or label check), so only pairs whose energy changed (the son's former
+// neighbours) or whose last entry had the other order are pushed; the pop
+// order, and so every merge, is the reference's.
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm) {
   const int GW = 2 * W + 1, GH = 2 * H + 1;
   int n = 0;
   for (size_t p = 0; p < (size_t)H * W; p++) n = std::max(n, part[p] + 1);
   for (size_t i = 0; i < (size_t)GH * GW; i++) ucm[i] = 0.0;
   if (n <= 0) return;
-  std::vector<int> label(n);
-  std::vector<Region> R(n);
-  for (int c = 0; c < n; c++) {
-    label[c] = c;
-    R[c].elements.push_back(c);
-  }
-  // boundary elements, visited in the reference's column-major pixel order
-  const int dx[4] = {1, 0, -1, 0}, dy[4] = {0, 1, 0, -1};
-  for (int y = 0; y < W; y++)
-    for (int x = 0; x < H; x++) {
-      const int a = part[(size_t)x * W + y];
-      if (a < 0) continue;  // a pixel outside every region (see the labelling); the reference indexes R[-1]
-      for (int v = 0; v < 4; v++) {
-        const int nx = x + dx[v], ny = y + dy[v];
-        if (nx < 0 || nx >= H || ny < 0 || ny >= W) continue;
-        const int b = part[(size_t)nx * W + ny];
-        if (b >= 0 && a != b) R[a].boundary.push_back({(x + nx + 1) * GW + (y + ny + 1), b});
+  std::vector<int> up(n);  // union-find; a root is a live region, its id the father's
+  for (int c = 0; c < n; c++) up[c] = c;
+  std::vector<Pair> P;
+  PairTable T((size_t)n * 4);
+  std::vector<std::vector<int32_t>> lists;
+  std::vector<double> raise;
+  std::vector<std::vector<int>> nb(n), pending(n);
+  // boundary coordinates, (odd, even) between horizontal neighbours and
+  // (even, odd) between vertical ones, gathered row by row and then put in
+  // the reference's column-major order before summing
+  for (int x = 0; x < H; x++)
+    for (int y = 0; y < W; y++) {
+      const int b = part[(size_t)x * W + y];
+      for (int side = 0; side < 2; side++) {
+        if (side == 0 ? y == 0 : x == 0) continue;
+        const int a = side == 0 ? part[(size_t)x * W + y - 1] : part[(size_t)(x - 1) * W + y];
+        if (a < 0 || b < 0 || a == b) continue;
+        const size_t np = P.size();
+        const int pi = T.find(a, b, &P);
+        if (P.size() != np) {
+          P[pi].list = (int)lists.size();
+          lists.emplace_back();
+          raise.push_back(-INFINITY);
+          nb[a].push_back(b);
+          nb[b].push_back(a);
+        }
+        const int gr = side == 0 ? 2 * x + 1 : 2 * x, gc = side == 0 ? 2 * y : 2 * y + 1;
+        lists[P[pi].list].push_back(gr * GW + gc);
       }
     }
-  std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> q;
-  std::vector<std::pair<int, int>> tmp;
-  for (int c = 0; c < n; c++) {
-    // the reference sorts by (neighbour, column-major coord) and sums in that order
-    tmp = R[c].boundary;
-    std::sort(tmp.begin(), tmp.end(), [&](const std::pair<int, int>& s, const std::pair<int, int>& t) {
-      if (s.second != t.second) return s.second < t.second;
-      const int cs = (s.first % GW) * GH + s.first / GW, ct = (t.first % GW) * GH + t.first / GW;
-      return cs < ct;
+  for (Pair& pr : P) {
+    std::vector<int32_t>& l = lists[pr.list];
+    std::sort(l.begin(), l.end(), [&](int32_t s0, int32_t s1) {
+      const int c0 = s0 % GW, c1 = s1 % GW;
+      return c0 != c1 ? c0 < c1 : s0 < s1;
     });
-    size_t i = 0;
-    while (i < tmp.size()) {
-      const int nb = tmp[i].second;
-      double total = 0, len = 0;
-      for (; i < tmp.size() && tmp[i].second == nb; i++) {
-        len++;
-        total += lb[tmp[i].first];
-      }
-      Nb& e = R[c].nbr[nb];
-      e.energy = total / len;
-      e.total = total;
-      e.length = len;
-      if (nb > c) q.push({total / len, c, nb});
+    for (int32_t c : l) {
+      pr.total += lb[c];
+      pr.length += 1.0;
     }
   }
+  std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> q;
+  auto push = [&](Pair& pr, double d, int a, int b) {  // entry (d, a, b); b is the region that pushes
+    q.push({d, a, b});
+    pr.pushed = d;
+    pr.first = a;
+    pending[a].push_back(b);
+  };
+  for (int c = 0; c < n; c++)
+    for (int k : nb[c])
+      if (k > c) {
+        Pair& pr = P[T.find(c, k, nullptr)];
+        pr.energy = pr.total / pr.length;
+        push(pr, pr.energy, c, k);
+      }
+  auto flush = [&](int l, double extra) {
+    const double r = std::max(raise[l], extra);
+    for (int32_t c : lists[l])
+      if (ucm[c] < r) ucm[c] = r;
+    std::vector<int32_t>().swap(lists[l]);
+  };
+  std::vector<int> touched;
   while (!q.empty()) {
     const Entry m = q.top();
     q.pop();
-    if (label[m.r1] != m.r1 || label[m.r2] != m.r2) continue;
-    const Nb& cur = R[m.r1].nbr[m.r2];  // inserts an empty entry where absent, as operator[] does
-    if (m.energy != cur.energy) continue;
-    const double saliency = cur.total / cur.length;
+    if (up[m.r1] != m.r1 || up[m.r2] != m.r2) continue;
+    const int ci = T.find(m.r1, m.r2, &P);  // creates an empty pair where absent, as operator[] does
+    if (m.energy != P[ci].energy) continue;
+    const double saliency = P[ci].total / P[ci].length;
     const int son = std::min(m.r1, m.r2), father = std::max(m.r1, m.r2);
-    Region &F = R[father], &S = R[son];
-    // son's boundary: raise the map, keep what does not face the father
-    // (elements that became interior carry the son's own label and are dropped)
-    std::vector<std::pair<int, int>> moved;
-    moved.reserve(S.boundary.size());
-    for (const auto& b : S.boundary) {
-      const int l = label[b.second];
-      if (l == son) continue;
-      if (ucm[b.first] < saliency) ucm[b.first] = saliency;
-      if (l != father) moved.push_back(b);
+    if (P[ci].list >= 0) flush(P[ci].list, saliency);  // the son-father boundary becomes interior
+    up[son] = father;
+    // the son's live neighbours other than the father join the father's
+    touched.clear();
+    for (int k : nb[son]) {
+      if (up[k] != k || k == father) continue;
+      const int si = T.find(son, k, nullptr);
+      const size_t np = P.size();
+      const int fi = T.find(father, k, &P);
+      if (P.size() != np) {
+        nb[father].push_back(k);
+        nb[k].push_back(father);
+      }
+      Pair &s = P[si], &f = P[fi];
+      f.total += s.total;
+      f.length += s.length;
+      raise[s.list] = std::max(raise[s.list], saliency);
+      if (f.list < 0) {
+        f.list = s.list;
+      } else {
+        int big = f.list, small = s.list;
+        if (lists[small].size() > lists[big].size()) std::swap(big, small);
+        const double r = raise[small];
+        for (int32_t c : lists[small])
+          if (ucm[c] < r) ucm[c] = r;
+        lists[big].insert(lists[big].end(), lists[small].begin(), lists[small].end());
+        std::vector<int32_t>().swap(lists[small]);
+        f.list = big;
+      }
+      touched.push_back(k);
     }
-    std::vector<std::pair<int, int>>().swap(S.boundary);
-    if (moved.size() > F.boundary.size()) moved.swap(F.boundary);
-    F.boundary.insert(F.boundary.end(), moved.begin(), moved.end());
-    for (int p : S.elements) label[p] = father;
-    if (S.elements.size() > F.elements.size()) S.elements.swap(F.elements);
-    F.elements.insert(F.elements.end(), S.elements.begin(), S.elements.end());
-    std::vector<int>().swap(S.elements);
-    for (auto it = F.nbr.begin(); it != F.nbr.end();) {
-      if (label[it->first] != it->first) it = F.nbr.erase(it);
-      else ++it;
+    std::vector<int>().swap(nb[son]);
+    std::vector<int>().swap(pending[son]);
+    for (int k : pending[father]) touched.push_back(k);
+    std::vector<int>().swap(pending[father]);
+    for (int k : touched) {
+      if (up[k] != k || k == father) continue;
+      const int fi = T.find(father, k, nullptr);
+      if (fi < 0) continue;
+      Pair& f = P[fi];
+      const double d = f.total / f.length;
+      f.energy = d;
+      if (!(f.pushed == d && f.first == k)) push(f, d, k, father);
     }
-    for (auto it = S.nbr.begin(); it != S.nbr.end();) {
-      if (label[it->first] != it->first || label[it->first] == father) it = S.nbr.erase(it);
-      else ++it;
-    }
-    for (const auto& kv : S.nbr) {
-      const int k = kv.first;
-      F.nbr[k].total += kv.second.total;
-      R[k].nbr[father].total += kv.second.total;
-      F.nbr[k].length += kv.second.length;
-      R[k].nbr[father].length += kv.second.length;
-    }
-    S.nbr.clear();
-    for (auto& kv : F.nbr) {
-      const double d = kv.second.total / kv.second.length;
-      q.push({d, kv.first, father});
-      kv.second.energy = d;
-      R[kv.first].nbr[father].energy = d;
+    if (nb[father].size() > 64) {  // drop merged-away neighbours now and then
+      std::vector<int>& v = nb[father];
+      size_t w = 0;
+      for (size_t r = 0; r < v.size(); r++)
+        if (up[v[r]] == v[r]) v[w++] = v[r];
+      v.resize(w);
     }
   }
+  for (size_t l = 0; l < lists.size(); l++)  // boundaries never closed (a split adjacency graph)
+    if (!lists[l].empty()) flush((int)l, -INFINITY);
   // CompleteContourMap: every even-even grid point takes the largest of its
   // four neighbours (starting from 0)
   for (int x = 0; x < GH; x += 2)
