@@ -267,8 +267,8 @@ def run_gpu(args):
                "regions": info["n_regions"], "edges": info["n_edges"], "artefacts": info["n_artefacts"]}
         if args.ucm_save:
             np.save(args.ucm_save, d_sor.cpu().numpy().reshape(8, 1024, 1024))
-            np.save(args.ucm_save[:-4] + "_map.npy" if args.ucm_save.endswith(".npy") else args.ucm_save + "_map",
-                    umap)
+            np.savez_compressed(args.ucm_save[:-4] + "_map.npz" if args.ucm_save.endswith(".npy")
+                                else args.ucm_save + "_map.npz", map=umap)
     achieved = (kb / kn) / (kms / kn / 1e3) / 1e9 if kn else None
     last = st_acc[-1]
     if rank == 0:
