@@ -126,6 +126,25 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def ucm_case():
+    """One batch, stitched to 1024 x 1024 on the device, then one gpb_ucm
+    call: the command behind the launch list of the OWT-UCM kernels."""
+    import torch
+    import gpb
+    _, cb, boxes, patches = make_workload()
+    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
+    ctx.compute_batch(patches)
+    places = [(x0, y0, ix, iy, iw, ih) for (y0, x0, h, w, iy, ix, ih, iw) in boxes]
+    # compute_batch leaves the batch's planes on the device; stitch them
+    d_nm = torch.empty(1024 * 1024, dtype=torch.float32, device="cuda")
+    d_or = torch.empty(8 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    ctx.stitch_device(gpb.STITCH_INTERIOR, 1024, 1024, places, d_nm.data_ptr(), d_or.data_ptr())
+    torch.cuda.synchronize()
+    _, info = ctx.ucm(None, d_orient=d_or.data_ptr(), shape=(1024, 1024))
+    print(json.dumps({"ucm_case": "done", "info": info}))
+    ctx.close()
+
+
 def ncu_case(eig="warm"):
     """One batch of the workload, nothing else: the command that ncu captures
     (a few launches of one kernel out of it).  eig="block" skips the coarse
@@ -317,11 +336,15 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-ucm", action="store_true")
+    ap.add_argument("--ucm-case", action="store_true", help="one batch and one OWT-UCM call only (for ncu)")
     ap.add_argument("--ucm-steps", type=int, default=3)
     ap.add_argument("--ucm-save", default=None, help="write the UCM input planes (.npy) to this path and the map beside it")
     ap.add_argument("--ncu-case", action="store_true", help="one batch only (for ncu captures)")
     ap.add_argument("--ncu-eig", default="warm", choices=["warm", "block"])
     args = ap.parse_args()
+    if args.ucm_case:
+        ucm_case()
+        return
     if args.ncu_case:
         ncu_case(args.ncu_eig)
     elif args.impl == "reference":
