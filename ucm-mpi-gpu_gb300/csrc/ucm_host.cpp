@@ -474,21 +474,37 @@ bool Contours::subdivide_global() {
   for (int round = 0;; round++) {
     if (round > 100000) return false;
     const size_t ne = edge.size(), nv = vert.size();
-    // cells of 16 x 16 pixels; a chord is listed in every cell its bounding box covers
-    const int CS = 16, GX = (H_ + CS - 1) / CS, GY = (W_ + CS - 1) / CS;
-    std::vector<std::vector<int>> cell((size_t)GX * GY);
-    for (size_t e = 0; e < ne; e++) {
-      const Vert &a = vert[edge[e].vs], &b = vert[edge[e].ve];
-      for (int cx = std::min(a.x, b.x) / CS; cx <= std::max(a.x, b.x) / CS; cx++)
-        for (int cy = std::min(a.y, b.y) / CS; cy <= std::max(a.y, b.y) / CS; cy++)
-          cell[(size_t)cx * GY + cy].push_back((int)e);
+    // cells of 8 x 8 pixels (CSR); a chord is listed in every cell its bounding box covers
+    const int CS = 8, GX = (H_ + CS - 1) / CS, GY = (W_ + CS - 1) / CS;
+    std::vector<int> cstart((size_t)GX * GY + 1, 0), cell_items;
+    for (int pass = 0; pass < 2; pass++) {
+      if (pass == 1) {
+        for (size_t c = 0; c < (size_t)GX * GY; c++) cstart[c + 1] += cstart[c];
+        cell_items.resize(cstart.back());
+      }
+      for (size_t e = 0; e < ne; e++) {
+        const Vert &a = vert[edge[e].vs], &b = vert[edge[e].ve];
+        for (int cx = std::min(a.x, b.x) / CS; cx <= std::max(a.x, b.x) / CS; cx++)
+          for (int cy = std::min(a.y, b.y) / CS; cy <= std::max(a.y, b.y) / CS; cy++) {
+            const size_t c = (size_t)cx * GY + cy;
+            if (pass == 0) cstart[c + 1]++;
+            else cell_items[cstart[c]++] = (int)e;
+          }
+      }
+      if (pass == 1)  // restore the starts
+        for (size_t c = (size_t)GX * GY; c > 0; c--) cstart[c] = cstart[c - 1];
+      if (pass == 1) cstart[0] = 0;
     }
+    auto cell_begin = [&](size_t c) { return cell_items.data() + cstart[c]; };
+    auto cell_end = [&](size_t c) { return cell_items.data() + cstart[c + 1]; };
     std::vector<uint8_t> mark(ne, 0);
     bool found = false;
     // (a) a vertex inside a chord's interior: every such chord is split
     for (size_t v = 0; v < nv; v++) {
       const i64 px = vert[v].x, py = vert[v].y;
-      for (int e : cell[(size_t)(px / CS) * GY + py / CS]) {
+      const size_t cv = (size_t)(px / CS) * GY + py / CS;
+      for (const int* it = cell_begin(cv); it != cell_end(cv); ++it) {
+        const int e = *it;
         const int a = edge[e].vs, b = edge[e].ve;
         if (a == (int)v || b == (int)v) continue;
         const i64 ax = vert[a].x, ay = vert[a].y, bx = vert[b].x, by = vert[b].y;
@@ -506,9 +522,10 @@ bool Contours::subdivide_global() {
     std::vector<std::pair<int, int>> pairs;
     for (int cx = 0; cx < GX; cx++)
       for (int cy = 0; cy < GY; cy++) {
-        const std::vector<int>& c = cell[(size_t)cx * GY + cy];
-        for (size_t i = 0; i < c.size(); i++)
-          for (size_t j = i + 1; j < c.size(); j++) {
+        const int* c = cell_begin((size_t)cx * GY + cy);
+        const size_t csz = (size_t)(cell_end((size_t)cx * GY + cy) - c);
+        for (size_t i = 0; i < csz; i++)
+          for (size_t j = i + 1; j < csz; j++) {
             const Vert &a0 = vert[edge[c[i]].vs], &a1 = vert[edge[c[i]].ve];
             const Vert &b0 = vert[edge[c[j]].vs], &b1 = vert[edge[c[j]].ve];
             const int lx = std::max(std::min(a0.x, a1.x), std::min(b0.x, b1.x));
@@ -685,6 +702,7 @@ class PairTable {
 struct Entry {
   double energy;
   int r1, r2;
+  int pair;  // index of the pair {r1, r2}, fixed while both regions live
   bool operator>(const Entry& o) const {  // the reference's (energy, region1, region2) order
     if (energy != o.energy) return energy > o.energy;
     if (r1 != o.r1) return r1 > o.r1;
@@ -730,10 +748,11 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
   PairTable T((size_t)n * 4);
   std::vector<std::vector<int32_t>> lists;
   std::vector<double> raise;
-  std::vector<std::vector<int>> nb(n), pending(n);
+  std::vector<std::vector<std::pair<int, int>>> nb(n), pending(n);  // (neighbour, pair index)
   // boundary coordinates, (odd, even) between horizontal neighbours and
   // (even, odd) between vertical ones, gathered row by row and then put in
   // the reference's column-major order before summing
+  int last_a[2] = {-1, -1}, last_b[2] = {-1, -1}, last_p[2] = {-1, -1};  // runs repeat a pair
   for (int x = 0; x < H; x++)
     for (int y = 0; y < W; y++) {
       const int b = part[(size_t)x * W + y];
@@ -742,13 +761,21 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
         const int a = side == 0 ? part[(size_t)x * W + y - 1] : part[(size_t)(x - 1) * W + y];
         if (a < 0 || b < 0 || a == b) continue;
         const size_t np = P.size();
-        const int pi = T.find(a, b, &P);
+        int pi;
+        if (a == last_a[side] && b == last_b[side]) {
+          pi = last_p[side];
+        } else {
+          pi = T.find(a, b, &P);
+          last_a[side] = a;
+          last_b[side] = b;
+          last_p[side] = pi;
+        }
         if (P.size() != np) {
           P[pi].list = (int)lists.size();
           lists.emplace_back();
           raise.push_back(-INFINITY);
-          nb[a].push_back(b);
-          nb[b].push_back(a);
+          nb[a].push_back({b, pi});
+          nb[b].push_back({a, pi});
         }
         const int gr = side == 0 ? 2 * x + 1 : 2 * x, gc = side == 0 ? 2 * y : 2 * y + 1;
         lists[P[pi].list].push_back(gr * GW + gc);
@@ -766,18 +793,18 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
     }
   }
   std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> q;
-  auto push = [&](Pair& pr, double d, int a, int b) {  // entry (d, a, b); b is the region that pushes
-    q.push({d, a, b});
-    pr.pushed = d;
-    pr.first = a;
-    pending[a].push_back(b);
+  auto push = [&](int pi, double d, int a, int b) {  // entry (d, a, b); b is the region that pushes
+    q.push({d, a, b, pi});
+    P[pi].pushed = d;
+    P[pi].first = a;
+    pending[a].push_back({b, pi});
   };
   for (int c = 0; c < n; c++)
-    for (int k : nb[c])
-      if (k > c) {
-        Pair& pr = P[T.find(c, k, nullptr)];
+    for (const auto& kp : nb[c])
+      if (kp.first > c) {
+        Pair& pr = P[kp.second];
         pr.energy = pr.total / pr.length;
-        push(pr, pr.energy, c, k);
+        push(kp.second, pr.energy, c, kp.first);
       }
   auto flush = [&](int l, double extra) {
     const double r = std::max(raise[l], extra);
@@ -785,12 +812,12 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
       if (ucm[c] < r) ucm[c] = r;
     std::vector<int32_t>().swap(lists[l]);
   };
-  std::vector<int> touched;
+  std::vector<std::pair<int, int>> touched;
   while (!q.empty()) {
     const Entry m = q.top();
     q.pop();
     if (up[m.r1] != m.r1 || up[m.r2] != m.r2) continue;
-    const int ci = T.find(m.r1, m.r2, &P);  // creates an empty pair where absent, as operator[] does
+    const int ci = m.pair;  // both regions live, so the pair is the one pushed
     if (m.energy != P[ci].energy) continue;
     const double saliency = P[ci].total / P[ci].length;
     const int son = std::min(m.r1, m.r2), father = std::max(m.r1, m.r2);
@@ -798,14 +825,14 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
     up[son] = father;
     // the son's live neighbours other than the father join the father's
     touched.clear();
-    for (int k : nb[son]) {
+    for (const auto& kp : nb[son]) {
+      const int k = kp.first, si = kp.second;
       if (up[k] != k || k == father) continue;
-      const int si = T.find(son, k, nullptr);
       const size_t np = P.size();
       const int fi = T.find(father, k, &P);
       if (P.size() != np) {
-        nb[father].push_back(k);
-        nb[k].push_back(father);
+        nb[father].push_back({k, fi});
+        nb[k].push_back({father, fi});
       }
       Pair &s = P[si], &f = P[fi];
       f.total += s.total;
@@ -823,26 +850,25 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
         std::vector<int32_t>().swap(lists[small]);
         f.list = big;
       }
-      touched.push_back(k);
+      touched.push_back({k, fi});
     }
-    std::vector<int>().swap(nb[son]);
-    std::vector<int>().swap(pending[son]);
-    for (int k : pending[father]) touched.push_back(k);
-    std::vector<int>().swap(pending[father]);
-    for (int k : touched) {
+    std::vector<std::pair<int, int>>().swap(nb[son]);
+    std::vector<std::pair<int, int>>().swap(pending[son]);
+    for (const auto& kp : pending[father]) touched.push_back(kp);
+    std::vector<std::pair<int, int>>().swap(pending[father]);
+    for (const auto& kp : touched) {
+      const int k = kp.first;
       if (up[k] != k || k == father) continue;
-      const int fi = T.find(father, k, nullptr);
-      if (fi < 0) continue;
-      Pair& f = P[fi];
+      Pair& f = P[kp.second];
       const double d = f.total / f.length;
       f.energy = d;
-      if (!(f.pushed == d && f.first == k)) push(f, d, k, father);
+      if (!(f.pushed == d && f.first == k)) push(kp.second, d, k, father);
     }
     if (nb[father].size() > 64) {  // drop merged-away neighbours now and then
-      std::vector<int>& v = nb[father];
+      std::vector<std::pair<int, int>>& v = nb[father];
       size_t w = 0;
       for (size_t r = 0; r < v.size(); r++)
-        if (up[v[r]] == v[r]) v[w++] = v[r];
+        if (up[v[r].first] == v[r].first) v[w++] = v[r];
       v.resize(w);
     }
   }
