@@ -119,3 +119,25 @@ def test_gpb_to_ucm_chain(orc):
     w2, lab, _, _ = uo.super_clean(uo.paint(g, vert, edges, off, px))
     assert np.abs(u2 - uo.normalize(uo.mean_pb(w2, lab))).max() <= UCM_TOL
     assert info["n_regions"] > 1 and u2.max() > 0
+
+
+def test_ucm_is_ultrametric_at_scale(ctx):
+    """Size-independent properties on a 640 x 512 image: values in [0, 1],
+    even-even points the max of their 4 neighbours, and the regions at a
+    higher threshold are unions of the regions at a lower one."""
+    import gpb
+    u2, info = ctx.ucm(_planes(640, 512, 51, 1.6))
+    assert info["fit_ok"] == 1 and 0.0 <= u2.min() and u2.max() <= 1.0
+    e = u2[2:-2:2, 2:-2:2]
+    nbr = np.maximum.reduce([u2[1:-3:2, 2:-2:2], u2[3:-1:2, 2:-2:2], u2[2:-2:2, 1:-3:2], u2[2:-2:2, 3:-1:2]])
+    assert np.array_equal(e, nbr)
+    prev = None
+    for k in (0.05, 0.15, 0.3, 0.6):
+        lab, n = gpb.ucm_labels_at_scale(u2, k)
+        if prev is not None:
+            pl, pn = prev
+            assert n <= pn
+            # every finer region maps into exactly one coarser region
+            pairs = np.unique(np.stack([pl.ravel(), lab.ravel()]), axis=1)
+            assert len(np.unique(pairs[0])) == pairs.shape[1]
+        prev = (lab, n)
