@@ -166,12 +166,11 @@ extern "C" gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, con
   const double ms_mid = ms_since(t2);
   // host: mean-boundary merge, calibration, output grid
   const auto t3 = std::chrono::steady_clock::now();
-  std::vector<double> lb(w2.begin(), w2.end()), um(N2);
-  ucm::mean_pb_merge(lb.data(), lab.data(), H, W, um.data());
-  ucm::normalize(um.data(), N2);
-  if (double_size) {
-    memcpy(ucm_out, um.data(), N2 * sizeof(double));
-  } else {
+  std::vector<double> um(double_size ? 0 : N2);
+  double* full = double_size ? ucm_out : um.data();  // the doubled grid is the caller's buffer where asked
+  ucm::mean_pb_merge(w2.data(), lab.data(), H, W, full);
+  ucm::normalize(full, N2);
+  if (!double_size) {
     const int GW = 2 * W + 1;
     for (int i = 0; i <= H; i++)
       for (int j = 0; j <= W; j++)

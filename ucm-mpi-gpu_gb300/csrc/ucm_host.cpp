@@ -736,7 +736,8 @@ struct Entry {
 // or label check), so only pairs whose energy changed (the son's former
 // neighbours) or whose last entry had the other order are pushed; the pop
 // order, and so every merge, is the reference's.
-void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm) {
+template <class T>
+static void merge_impl(const T* lb, const int32_t* part, int H, int W, double* ucm) {
   const int GW = 2 * W + 1, GH = 2 * H + 1;
   int n = 0;
   for (size_t p = 0; p < (size_t)H * W; p++) n = std::max(n, part[p] + 1);
@@ -788,7 +789,7 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
       return c0 != c1 ? c0 < c1 : s0 < s1;
     });
     for (int32_t c : l) {
-      pr.total += lb[c];
+      pr.total += (double)lb[c];
       pr.length += 1.0;
     }
   }
@@ -887,14 +888,39 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
     }
 }
 
+void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm) {
+  merge_impl(lb, part, H, W, ucm);
+}
+
+// the same on float strengths (as the device grid holds them; widened exactly)
+void mean_pb_merge(const float* lb, const int32_t* part, int H, int W, double* ucm) {
+  merge_impl(lb, part, H, W, ucm);
+}
+
 // NormalizeOutput (contours2ucm.cpp:191-249): logistic calibration of the
 // mean boundary strength, rescaled and clipped to [0, 1].
+// Most of the grid is 0 and boundary runs repeat one value, so a value
+// equal to the previous one reuses its result (the same arithmetic either way).
 void normalize(double* u, size_t n) {
-  for (size_t i = 0; i < n; i++) {
-    const double z = 0.0 + 1.0 * -2.7487 + u[i] * 11.1189;
+  auto f = [](double x) {
+    const double z = 0.0 + 1.0 * -2.7487 + x * 11.1189;
     double v = 1.0 / (1.0 + exp(-z));
     v = (v - 0.0602) / (1.0 - 0.0602);
-    u[i] = std::min(1.0, std::max(0.0, v));
+    return std::min(1.0, std::max(0.0, v));
+  };
+  const double f0 = f(0.0);
+  double last_in = 0.0, last_out = f0;
+  for (size_t i = 0; i < n; i++) {
+    const double x = u[i];
+    if (x == 0.0) {
+      u[i] = f0;
+    } else if (x == last_in) {
+      u[i] = last_out;
+    } else {
+      last_in = x;
+      last_out = f(x);
+      u[i] = last_out;
+    }
   }
 }
 

@@ -19,6 +19,7 @@ uint32_t components8(const uint8_t* bw, int H, int W, std::vector<uint32_t>& lab
 bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out);
 int edge_orientation(int x1, int y1, int x2, int y2);
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm);
+void mean_pb_merge(const float* lb, const int32_t* part, int H, int W, double* ucm);
 void normalize(double* u, size_t n);
 
 }  // namespace ucm
