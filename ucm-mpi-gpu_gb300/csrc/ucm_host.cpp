@@ -736,8 +736,8 @@ struct Entry {
 // or label check), so only pairs whose energy changed (the son's former
 // neighbours) or whose last entry had the other order are pushed; the pop
 // order, and so every merge, is the reference's.
-template <class T>
-static void merge_impl(const T* lb, const int32_t* part, int H, int W, double* ucm) {
+template <class Real>
+static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double* ucm) {
   const int GW = 2 * W + 1, GH = 2 * H + 1;
   int n = 0;
   for (size_t p = 0; p < (size_t)H * W; p++) n = std::max(n, part[p] + 1);
