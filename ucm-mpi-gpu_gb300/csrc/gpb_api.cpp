@@ -212,7 +212,6 @@ struct gpb_ctx {
   uint64_t token = 0;          // identifies this context's constant tables
   Buf b;
   std::string last_error;
-  bool host_dense = getenv("GPB_HOST_DENSE") != nullptr;  // 32 x 32 eigensolver steps on the host
   // device scratch of the OWT-UCM stage (ucm_api.cpp), freed with the context
   void* ucm_state = nullptr;
   void (*ucm_free)(void*) = nullptr;
@@ -995,59 +994,45 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   };
   // orthonormalise F twice, then Rayleigh-Ritz on span(F); AF receives A F
   // comp: compensated Rayleigh-Ritz product and rotation (see cf_step_t, cf_rotate)
-  // The 32 x 32 steps run on the device (cf_dense) unless GPB_HOST_DENSE is
-  // set, which keeps them on the host thread pool (FP64, eig_host.cpp); the
-  // device path leaves one host round trip per call, for the residuals and
-  // Ritz values that steer the next filter.
   auto rr = [&](float* F, float* AF, bool comp) -> gpb_status {
     for (int pass = 0; pass < 2; pass++) {
       CK(cf_launch_gram(a, nt, F, F, b.bgram, s));
-      if (ctx->host_dense) {
-        CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        ctx->host_pool().run(np, [&](int i) {
-          if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
-        });
-        CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
-      } else {
-        CK(cf_launch_dense(np, b.active, b.bgram, 0, b.bmat, b.btheta, s));
-        ctx->launches++;
-      }
+      CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      ctx->host_pool().run(np, [&](int i) {
+        if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
+      });
+      if (ctx->trace && active[0])
+        fprintf(stderr, "[gpb] gram pass %d patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", pass, G[0],
+                G[kBlk + 1], G[BB - 1], M[0]);
+      CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
       CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
       ctx->launches += 2;
     }
     CK(upload_unit());
     CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s, comp));
     CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
+    CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     ctx->launches += 2;
-    if (ctx->host_dense) {
-      CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      ctx->host_pool().run(np, [&](int i) {
-        if (!active[i]) return;
-        std::vector<double> H(BB), w(kBlk), Zm(BB);
-        for (int r = 0; r < kBlk; r++)
-          for (int c = 0; c < kBlk; c++)
-            H[r * kBlk + c] = 0.5 * (G[i * BB + r * kBlk + c] + G[i * BB + c * kBlk + r]);
-        gpb::sym_eig(H.data(), kBlk, w.data(), Zm.data());
-        for (int c = 0; c < kBlk; c++) theta[(size_t)i * kBlk + c] = w[c];
-        std::copy(Zm.begin(), Zm.end(), M.begin() + i * BB);
-      });
-      CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(b.btheta, theta.data(), theta.size() * sizeof(double), cudaMemcpyHostToDevice, s));
-    } else {
-      CK(cf_launch_dense(np, b.active, b.bgram, 1, b.bmat, b.btheta, s));
-      ctx->launches++;
-    }
+    ctx->host_pool().run(np, [&](int i) {
+      if (!active[i]) return;
+      mv[i] += kBlk;
+      std::vector<double> H(BB), w(kBlk), Zm(BB);
+      for (int r = 0; r < kBlk; r++)
+        for (int c = 0; c < kBlk; c++)
+          H[r * kBlk + c] = 0.5 * (G[i * BB + r * kBlk + c] + G[i * BB + c * kBlk + r]);
+      gpb::sym_eig(H.data(), kBlk, w.data(), Zm.data());
+      for (int c = 0; c < kBlk; c++) theta[(size_t)i * kBlk + c] = w[c];
+      std::copy(Zm.begin(), Zm.end(), M.begin() + i * BB);
+    });
+    CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(b.btheta, theta.data(), theta.size() * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cf_launch_rotate(a, nt, F, AF, kBlk, s, comp));
     CK(cf_launch_resid(a, nt, F, AF, b.bres, s));
     CK(cudaMemcpyAsync(res.data(), b.bres, res.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (!ctx->host_dense)
-      CK(cudaMemcpyAsync(theta.data(), b.btheta, theta.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     ctx->launches += 2;
-    for (int i = 0; i < np; i++)
-      if (active[i]) mv[i] += kBlk;
     return GPB_OK;
   };
   gpb_status st = rr(X, AX, false);

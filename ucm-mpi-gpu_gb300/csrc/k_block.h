@@ -66,8 +66,5 @@ cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const 
 cudaError_t cf_launch_extract(const BlkArgs& a, int ntiles, const float* X, float* evec, int nvec,
                               cudaStream_t s);
 cudaError_t cf_launch_init(const BlkArgs& a, int ntiles, float* X, cudaStream_t s);
-// mode 0: M = G^-1/2 (symmetric part, eigenvalues clamped); mode 1: theta, M = eigenpairs ascending
-cudaError_t cf_launch_dense(int npatch, const int* active, const double* G, int mode, double* M, double* theta,
-                            cudaStream_t s);
 
 }  // namespace gpb
