@@ -274,14 +274,25 @@ typedef struct {
 gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, const float* orient, int orient_on_device,
                    int double_size, double* ucm_out, gpb_ucm_info* info);
 
-/* Intermediates of the last gpb_ucm call on this context, copied to host:
+/* The same for n images at once: the pieces the reference hands to one MPI
+ * rank each (src/main.cpp:456-459).  They are flooded together (one CTA
+ * each); their contour fitting and merging run on the context's host
+ * threads, one image per thread.  widths, heights, orient and ucm_out have
+ * n entries, info n entries or NULL.  The doubled grids of all images
+ * together must stay below 2^31 cells. */
+gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                         const float* const* orient, int orient_on_device, int double_size, double* const* ucm_out,
+                         gpb_ucm_info* info);
+
+/* Intermediates of image `image` of the last gpb_ucm / gpb_ucm_batch call on
+ * this context, copied to host:
  * GPB_UCM_QUANT   u8, H x W: the 8-bit max-over-orientations image
  * GPB_UCM_ARCS    u8, H x W: 1 on watershed pixels
  * GPB_UCM_WSWT    float, H x W: contour strength painted along the edges
  * GPB_UCM_WSWT2   float, (2H+1) x (2W+1): the cleaned doubled grid ws_wt2
  * GPB_UCM_REGIONS int32, H x W: region ids of the finest partition */
 enum { GPB_UCM_QUANT = 0, GPB_UCM_ARCS = 1, GPB_UCM_WSWT = 2, GPB_UCM_WSWT2 = 3, GPB_UCM_REGIONS = 4 };
-gpb_status gpb_ucm_fetch(gpb_ctx* ctx, int what, void* host, size_t bytes);
+gpb_status gpb_ucm_fetch(gpb_ctx* ctx, size_t image, int what, void* host, size_t bytes);
 
 /* The host stages, usable without a device.
  * gpb_ucm_fit_contours: fit_contour (src/fit_contour.cpp) of a 0/1 map of

@@ -141,3 +141,24 @@ def test_ucm_is_ultrametric_at_scale(ctx):
             pairs = np.unique(np.stack([pl.ravel(), lab.ravel()]), axis=1)
             assert len(np.unique(pairs[0])) == pairs.shape[1]
         prev = (lab, n)
+
+
+def test_ucm_batch_equals_single_calls(ctx):
+    """A batch of uneven images (flooded together, fitted and merged on
+    the host threads) gives each image the map and intermediates of its
+    own single call."""
+    import gpb
+    shapes = [(64, 80, 61), (33, 47, 62), (150, 120, 63), (40, 40, 64), (97, 30, 65)]
+    planes = [_planes(h, w, s, 1.3) for (h, w, s) in shapes]
+    got = ctx.ucm_batch(planes)
+    arcs_b = [ctx.ucm_fetch(gpb.UCM_ARCS, i) for i in range(len(planes))]
+    regs_b = [ctx.ucm_fetch(gpb.UCM_REGIONS, i) for i in range(len(planes))]
+    for i, p in enumerate(planes):
+        u, info = ctx.ucm(p)
+        assert np.array_equal(got[i][0], u)
+        assert got[i][1]["n_regions"] == info["n_regions"] and got[i][1]["n_edges"] == info["n_edges"]
+        assert np.array_equal(arcs_b[i], ctx.ucm_fetch(gpb.UCM_ARCS))
+        assert np.array_equal(regs_b[i], ctx.ucm_fetch(gpb.UCM_REGIONS))
+    small = ctx.ucm_batch(planes[:2], double_size=False)
+    for i in range(2):
+        assert np.array_equal(small[i][0], ctx.ucm(planes[i], double_size=False)[0])

@@ -1610,6 +1610,7 @@ namespace gpb {
 int ctx_device(gpb_ctx* c) { return c->device; }
 cudaStream_t ctx_stream(gpb_ctx* c) { return c->st; }
 void ctx_set_error(gpb_ctx* c, const char* m) { c->last_error = m; }
+void ctx_parallel_for(gpb_ctx* c, int n, const std::function<void(int)>& f) { c->host_pool().run(n, f); }
 void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*)) {
   c->ucm_free = release;
   return c->ucm_state;

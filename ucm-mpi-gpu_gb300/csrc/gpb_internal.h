@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <vector>
 
 struct gpb_ctx;
@@ -92,5 +93,6 @@ int ctx_device(gpb_ctx* c);
 cudaStream_t ctx_stream(gpb_ctx* c);
 void ctx_set_error(gpb_ctx* c, const char* m);
 void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*));
+void ctx_parallel_for(gpb_ctx* c, int n, const std::function<void(int)>& f);  // f(0..n-1) on the host pool
 
 }  // namespace gpb

@@ -23,8 +23,8 @@
 //   k_ucm_finish   region labels of the pixels and the padded strength grid
 //                  ws_wt2 (contours2ucm.cpp:439-458)
 //
-// Images are processed one per CTA where a stage is sequential per image
-// (flooding, artefact fixes); elsewhere grid-stride over the image.
+// The flooding runs one CTA per image over a batch; the other stages run
+// per image, grid-stride over it (the artefact fixes in one thread).
 #include <stdint.h>
 
 #include "ucm_dev.h"
@@ -459,7 +459,7 @@ static int grid_for(long long n) {
   return (int)(g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g));
 }
 
-cudaError_t ucm_front(const float* d_orient, int H, int W, UcmScratch& s, cudaStream_t st) {
+cudaError_t ucm_prepare(const float* d_orient, int H, int W, UcmScratch& s, cudaStream_t st) {
   const long long N = (long long)H * W;
   cudaError_t e = cudaMemsetAsync(s.mm, 0, 2 * sizeof(unsigned), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.mm, 0xff, sizeof(unsigned), st);
@@ -467,8 +467,12 @@ cudaError_t ucm_front(const float* d_orient, int H, int W, UcmScratch& s, cudaSt
   k_ucm_pbmax<<<grid_for(N), 256, 0, st>>>(d_orient, N, s.pb, s.mm);
   k_ucm_quant<<<grid_for(N), 256, 0, st>>>(s.pb, N, s.mm, s.q);
   k_ws_rowsort<<<H, 32, 0, st>>>(s.q, H, W, s.off, s.cols);
-  k_ws_flood<<<1, 1024, 0, st>>>(s.img, s.off, s.cols, s.ws);
-  k_ws_bw<<<grid_for(N), 256, 0, st>>>(s.ws, N, s.bw);
+  return cudaGetLastError();
+}
+
+cudaError_t ucm_flood(int nimg, long long total_pix, const UcmScratch& base, cudaStream_t st) {
+  k_ws_flood<<<nimg, 1024, 0, st>>>(base.img, base.off, base.cols, base.ws);
+  k_ws_bw<<<grid_for(total_pix), 256, 0, st>>>(base.ws, total_pix, base.bw);
   return cudaGetLastError();
 }
 

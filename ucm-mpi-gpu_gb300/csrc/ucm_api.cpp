@@ -1,10 +1,17 @@
 // ucm_api.cpp -- the C ABI of the OWT-UCM stage: device stages (k_ucm.cu)
 // around the host stages (ucm_host.cpp), in the order of Contours2Ucm
 // (src/contours2ucm.cpp:405-490).
+//
+// A call takes a batch of images, the pieces that the reference gives to
+// one MPI rank each (src/main.cpp:456-459): the images are flooded together
+// (one CTA each), their contour fitting and merging run on the context's
+// host thread pool, one image per thread, and the data-parallel stages run
+// image after image on the context's stream.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <vector>
 
@@ -17,34 +24,68 @@ using namespace gpb;
 
 namespace {
 
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// where image i's slices start in the batch's concatenated arrays
+struct Offsets {
+  size_t pix, pix4, rows, rows2, grid2, bsum;
+};
+
 struct UcmState {
-  UcmScratch s{};
   void* base = nullptr;
-  size_t cap = 0;          // bytes of base
-  size_t cap_paint = 0;    // entries of the paint list
-  float* orient = nullptr; // staging of host planes
+  size_t cap = 0;           // bytes of base
+  int32_t* paint_pix = nullptr;
+  size_t cap_pix = 0;       // entries of the paint list
+  uint8_t* paint_ori = nullptr;
+  size_t cap_ori = 0;
+  float* orient = nullptr;  // staging of host planes
   size_t cap_orient = 0;
-  int H = 0, W = 0;        // the last call's image
+  std::vector<UcmScratch> views;  // image i's slices of the batch arrays
+  std::vector<int> H, W;          // the last call's images
 };
 
 void ucm_release(void* p) {
   UcmState* u = (UcmState*)p;
   if (!u) return;
   cudaFree(u->base);
-  cudaFree(u->s.paint_pix);
-  cudaFree(u->s.paint_ori);
+  cudaFree(u->paint_pix);
+  cudaFree(u->paint_ori);
   cudaFree(u->orient);
   delete u;
 }
 
-size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+template <class T>
+cudaError_t grow_dev(T*& p, size_t& cap, size_t need) {
+  if (need <= cap && p) return cudaSuccess;
+  cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc(&p, std::max<size_t>(need, 1) * sizeof(T));
+  if (e == cudaSuccess) cap = need;
+  return e;
+}
 
-// carve the fixed-size scratch of an H x W image out of one allocation
-cudaError_t ucm_reserve(UcmState& u, int H, int W) {
-  const size_t N = (size_t)H * W, N4 = 4 * N, N2 = (size_t)(2 * H + 1) * (2 * W + 1);
-  const size_t sizes[] = {2 * sizeof(unsigned), N * 4, N, (size_t)H * 257 * 4, N * 2, sizeof(UcmImage), N * 4, N,
-                          N * 4, N4 * 4, (size_t)(2 * H + 1) * 4, 4, N4 * 4, N4 * 4, N4 * 4,
-                          (N4 / 4096 + 2) * 4, 4, N * 4, N2 * 4};
+// one allocation for the batch; every per-image array is a slice of a
+// concatenated array, so one kernel can sweep several images at once
+cudaError_t ucm_reserve(UcmState& u, const std::vector<int>& H, const std::vector<int>& W) {
+  const size_t n = H.size();
+  std::vector<Offsets> off(n + 1);
+  off[0] = {0, 0, 0, 0, 0, 0};
+  for (size_t i = 0; i < n; i++) {
+    const size_t N = (size_t)H[i] * W[i];
+    off[i + 1].pix = off[i].pix + N;
+    off[i + 1].pix4 = off[i].pix4 + 4 * N;
+    off[i + 1].rows = off[i].rows + H[i];
+    off[i + 1].rows2 = off[i].rows2 + 2 * H[i] + 1;
+    off[i + 1].grid2 = off[i].grid2 + (size_t)(2 * H[i] + 1) * (2 * W[i] + 1);
+    off[i + 1].bsum = off[i].bsum + 4 * N / 4096 + 2;
+  }
+  const Offsets& T = off[n];
+  // slots: mm, pb, q, off, cols, img, ws, bw, wswt, pb2, rowcnt, nart, art, par, rank, bsum, nreg, labels, wswt2
+  const size_t sizes[] = {2 * n * 4, T.pix * 4, T.pix, T.rows * 257 * 4, T.pix * 2, n * sizeof(UcmImage), T.pix * 4,
+                          T.pix, T.pix * 4, T.pix4 * 4, T.rows2 * 4, n * 4, T.pix4 * 4, T.pix4 * 4, T.pix4 * 4,
+                          T.bsum * 4, n * 4, T.pix * 4, T.grid2 * 4};
+  constexpr size_t kSlots = sizeof(sizes) / sizeof(sizes[0]);
   size_t need = 0;
   for (size_t b : sizes) need += align256(b);
   if (need > u.cap) {
@@ -55,15 +96,35 @@ cudaError_t ucm_reserve(UcmState& u, int H, int W) {
     if (e != cudaSuccess) return e;
     u.cap = need;
   }
+  char* base[kSlots];
   char* p = (char*)u.base;
-  void** slots[] = {(void**)&u.s.mm,   (void**)&u.s.pb,     (void**)&u.s.q,      (void**)&u.s.off,
-                    (void**)&u.s.cols, (void**)&u.s.img,    (void**)&u.s.ws,     (void**)&u.s.bw,
-                    (void**)&u.s.wswt, (void**)&u.s.pb2,    (void**)&u.s.rowcnt, (void**)&u.s.nart,
-                    (void**)&u.s.art,  (void**)&u.s.par,    (void**)&u.s.rank,   (void**)&u.s.bsum,
-                    (void**)&u.s.nreg, (void**)&u.s.labels, (void**)&u.s.wswt2};
-  for (size_t k = 0; k < sizeof(sizes) / sizeof(sizes[0]); k++) {
-    *slots[k] = p;
+  for (size_t k = 0; k < kSlots; k++) {
+    base[k] = p;
     p += align256(sizes[k]);
+  }
+  u.views.assign(n, UcmScratch{});
+  for (size_t i = 0; i < n; i++) {
+    const Offsets& o = off[i];
+    UcmScratch& v = u.views[i];
+    v.mm = (unsigned*)base[0] + 2 * i;
+    v.pb = (float*)base[1] + o.pix;
+    v.q = (uint8_t*)base[2] + o.pix;
+    v.off = (int32_t*)base[3] + o.rows * 257;
+    v.cols = (uint16_t*)base[4] + o.pix;
+    v.img = (UcmImage*)base[5] + i;
+    v.ws = (int32_t*)base[6] + o.pix;
+    v.bw = (uint8_t*)base[7] + o.pix;
+    v.wswt = (float*)base[8] + o.pix;
+    v.pb2 = (float*)base[9] + o.pix4;
+    v.rowcnt = (int32_t*)base[10] + o.rows2;
+    v.nart = (int32_t*)base[11] + i;
+    v.art = (int32_t*)base[12] + o.pix4;
+    v.par = (int32_t*)base[13] + o.pix4;
+    v.rank = (int32_t*)base[14] + o.pix4;
+    v.bsum = (int32_t*)base[15] + o.bsum;
+    v.nreg = (int32_t*)base[16] + i;
+    v.labels = (int32_t*)base[17] + o.pix;
+    v.wswt2 = (float*)base[18] + o.grid2;
   }
   return cudaSuccess;
 }
@@ -74,122 +135,181 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
 
 }  // namespace
 
-#define UCK(x)                                      \
-  do {                                              \
-    cudaError_t e_ = (x);                           \
-    if (e_ != cudaSuccess) {                        \
-      ctx_set_error(ctx, cudaGetErrorString(e_));   \
+#define UCK(x)                                                               \
+  do {                                                                       \
+    cudaError_t e_ = (x);                                                    \
+    if (e_ != cudaSuccess) {                                                 \
+      ctx_set_error(ctx, cudaGetErrorString(e_));                            \
       return e_ == cudaErrorMemoryAllocation ? GPB_ERR_NOMEM : GPB_ERR_CUDA; \
-    }                                               \
+    }                                                                        \
   } while (0)
 
-extern "C" gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, const float* orient,
-                              int orient_on_device, int double_size, double* ucm_out, gpb_ucm_info* info) {
-  if (!ctx || !orient || !ucm_out || width < 2 || height < 2 || width > 65535 || height > 65535) return GPB_ERR_ARG;
-  if (4ull * width * height >= (1ull << 31)) return GPB_ERR_ARG;  // int32 indices of the doubled grid
+extern "C" gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                    const float* const* orient, int orient_on_device, int double_size,
+                                    double* const* ucm_out, gpb_ucm_info* info) {
+  if (!ctx || n == 0 || n > 65535 || !widths || !heights || !orient || !ucm_out) return GPB_ERR_ARG;
+  size_t total4 = 0;
+  for (size_t i = 0; i < n; i++) {
+    const uint32_t w = widths[i], h = heights[i];
+    if (!orient[i] || !ucm_out[i] || w < 2 || h < 2 || w > 65535 || h > 65535) return GPB_ERR_ARG;
+    total4 += 4ull * w * h;
+  }
+  if (total4 >= (1ull << 31)) return GPB_ERR_ARG;  // int32 indices of the doubled grids
   const auto t0 = std::chrono::steady_clock::now();
-  const int H = (int)height, W = (int)width;
-  const size_t N = (size_t)H * W;
+  const int ni = (int)n;
+  std::vector<int> H(n), W(n);
+  std::vector<size_t> N(n), pix(n + 1, 0);
+  for (size_t i = 0; i < n; i++) {
+    H[i] = (int)heights[i];
+    W[i] = (int)widths[i];
+    N[i] = (size_t)H[i] * W[i];
+    pix[i + 1] = pix[i] + N[i];
+  }
   UCK(cudaSetDevice(ctx_device(ctx)));
   cudaStream_t st = ctx_stream(ctx);
   void*& slot = ctx_ucm_state(ctx, ucm_release);
   if (!slot) slot = new UcmState();
   UcmState& u = *(UcmState*)slot;
+  u.H.clear();
+  u.W.clear();
   UCK(ucm_reserve(u, H, W));
-  u.H = 0;
-  u.W = 0;
-  const float* d_orient = orient;
-  if (!orient_on_device) {
-    if (u.cap_orient < 8 * N) {
-      cudaFree(u.orient);
-      u.orient = nullptr;
-      u.cap_orient = 0;
-      UCK(cudaMalloc(&u.orient, 8 * N * sizeof(float)));
-      u.cap_orient = 8 * N;
+  std::vector<const float*> d_orient(n);
+  if (orient_on_device) {
+    for (size_t i = 0; i < n; i++) d_orient[i] = orient[i];
+  } else {
+    UCK(grow_dev(u.orient, u.cap_orient, 8 * pix[n]));
+    for (size_t i = 0; i < n; i++) {
+      d_orient[i] = u.orient + 8 * pix[i];
+      UCK(cudaMemcpyAsync(u.orient + 8 * pix[i], orient[i], 8 * N[i] * sizeof(float), cudaMemcpyHostToDevice, st));
     }
-    UCK(cudaMemcpyAsync(u.orient, orient, 8 * N * sizeof(float), cudaMemcpyHostToDevice, st));
-    d_orient = u.orient;
   }
-  const UcmImage img{H, W, 0, 0};
-  UCK(cudaMemcpyAsync(u.s.img, &img, sizeof(img), cudaMemcpyHostToDevice, st));
-  // device: orientation max, quantisation, flooding
-  UCK(ucm_front(d_orient, H, W, u.s, st));
-  std::vector<uint8_t> bw(N);
-  UCK(cudaMemcpyAsync(bw.data(), u.s.bw, N, cudaMemcpyDeviceToHost, st));
+  std::vector<UcmImage> imgs(n);
+  for (size_t i = 0; i < n; i++)
+    imgs[i] = {H[i], W[i], (long long)pix[i], (int)((u.views[i].off - u.views[0].off) / 257)};
+  UCK(cudaMemcpyAsync(u.views[0].img, imgs.data(), n * sizeof(UcmImage), cudaMemcpyHostToDevice, st));
+  // device: orientation max, quantisation and row sort per image, then one flooding launch for all
+  for (size_t i = 0; i < n; i++) UCK(ucm_prepare(d_orient[i], H[i], W[i], u.views[i], st));
+  UCK(ucm_flood(ni, (long long)pix[n], u.views[0], st));
+  std::vector<uint8_t> bw(pix[n]);
+  UCK(cudaMemcpyAsync(bw.data(), u.views[0].bw, pix[n], cudaMemcpyDeviceToHost, st));
   UCK(cudaStreamSynchronize(st));
   const double ms_front = ms_since(t0);
-  // host: contour fitting, then the list of painted pixels
+  // host: contour fitting and the painted pixels, one image per thread
   const auto t1 = std::chrono::steady_clock::now();
-  ucm::FitResult fit;
-  const bool ok = ucm::fit_contours(bw.data(), H, W, fit);
-  const int ne = (int)fit.es.size();
-  std::vector<int32_t> ppix;
-  std::vector<uint8_t> pori;
-  ppix.reserve(fit.px.size() + 2 * ne);
-  pori.reserve(fit.px.size() + 2 * ne);
-  for (int e = 0; e < ne; e++) {
-    const int a = fit.es[e], b = fit.ee[e];
-    const uint8_t o = (uint8_t)ucm::edge_orientation(fit.vx[a], fit.vy[a], fit.vx[b], fit.vy[b]);
-    for (int k = fit.off[e]; k < fit.off[e + 1]; k++) ppix.push_back(fit.px[k]), pori.push_back(o);
-    ppix.push_back(fit.vx[a] * W + fit.vy[a]), pori.push_back(o);
-    ppix.push_back(fit.vx[b] * W + fit.vy[b]), pori.push_back(o);
-  }
+  std::vector<ucm::FitResult> fit(n);
+  std::vector<char> ok(n);
+  std::vector<std::vector<int32_t>> ppix(n);
+  std::vector<std::vector<uint8_t>> pori(n);
+  std::vector<double> ms_fit_i(n);
+  ctx_parallel_for(ctx, ni, [&](int i) {
+    const auto ti = std::chrono::steady_clock::now();
+    ok[i] = ucm::fit_contours(bw.data() + pix[i], H[i], W[i], fit[i]);
+    const ucm::FitResult& f = fit[i];
+    const int ne = (int)f.es.size();
+    ppix[i].reserve(f.px.size() + 2 * ne);
+    pori[i].reserve(f.px.size() + 2 * ne);
+    for (int e = 0; e < ne; e++) {
+      const int a = f.es[e], b = f.ee[e];
+      const uint8_t o = (uint8_t)ucm::edge_orientation(f.vx[a], f.vy[a], f.vx[b], f.vy[b]);
+      for (int k = f.off[e]; k < f.off[e + 1]; k++) ppix[i].push_back(f.px[k]), pori[i].push_back(o);
+      ppix[i].push_back(f.vx[a] * W[i] + f.vy[a]), pori[i].push_back(o);
+      ppix[i].push_back(f.vx[b] * W[i] + f.vy[b]), pori[i].push_back(o);
+    }
+    ms_fit_i[i] = ms_since(ti);
+  });
   const double ms_fit = ms_since(t1);
-  // device: painting, super contour, cleaning, labelling
+  // device: painting, super contour, cleaning, labelling, image after image
   const auto t2 = std::chrono::steady_clock::now();
-  const int np = (int)ppix.size();
-  if ((size_t)np > u.cap_paint) {
-    cudaFree(u.s.paint_pix);
-    cudaFree(u.s.paint_ori);
-    u.s.paint_pix = nullptr;
-    u.s.paint_ori = nullptr;
-    u.cap_paint = 0;
-    UCK(cudaMalloc(&u.s.paint_pix, (size_t)np * sizeof(int32_t)));
-    UCK(cudaMalloc(&u.s.paint_ori, (size_t)np));
-    u.cap_paint = (size_t)np;
+  std::vector<size_t> poff(n + 1, 0);
+  for (size_t i = 0; i < n; i++) poff[i + 1] = poff[i] + ppix[i].size();
+  UCK(grow_dev(u.paint_pix, u.cap_pix, poff[n]));
+  UCK(grow_dev(u.paint_ori, u.cap_ori, poff[n]));
+  for (size_t i = 0; i < n; i++) {
+    const int np = (int)ppix[i].size();
+    if (np) {
+      UCK(cudaMemcpyAsync(u.paint_pix + poff[i], ppix[i].data(), (size_t)np * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, st));
+      UCK(cudaMemcpyAsync(u.paint_ori + poff[i], pori[i].data(), (size_t)np, cudaMemcpyHostToDevice, st));
+    }
+    UcmScratch v = u.views[i];
+    v.paint_pix = u.paint_pix + poff[i];
+    v.paint_ori = u.paint_ori + poff[i];
+    UCK(ucm_paint(d_orient[i], H[i], W[i], np, v, st));
+    UCK(ucm_mid(H[i], W[i], v, st));
   }
-  if (np) {
-    UCK(cudaMemcpyAsync(u.s.paint_pix, ppix.data(), (size_t)np * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    UCK(cudaMemcpyAsync(u.s.paint_ori, pori.data(), (size_t)np, cudaMemcpyHostToDevice, st));
-  }
-  UCK(ucm_paint(d_orient, H, W, np, u.s, st));
-  UCK(ucm_mid(H, W, u.s, st));
-  const size_t N2 = (size_t)(2 * H + 1) * (2 * W + 1);
-  std::vector<float> w2(N2);
-  std::vector<int32_t> lab(N);
-  int32_t counts[2] = {0, 0};
-  UCK(cudaMemcpyAsync(w2.data(), u.s.wswt2, N2 * sizeof(float), cudaMemcpyDeviceToHost, st));
-  UCK(cudaMemcpyAsync(lab.data(), u.s.labels, N * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  UCK(cudaMemcpyAsync(counts, u.s.nreg, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  UCK(cudaMemcpyAsync(counts + 1, u.s.nart, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  std::vector<size_t> g2(n + 1, 0);
+  for (size_t i = 0; i < n; i++) g2[i + 1] = g2[i] + (size_t)(2 * H[i] + 1) * (2 * W[i] + 1);
+  std::vector<float> w2(g2[n]);
+  std::vector<int32_t> lab(pix[n]), counts(2 * n);
+  UCK(cudaMemcpyAsync(w2.data(), u.views[0].wswt2, g2[n] * sizeof(float), cudaMemcpyDeviceToHost, st));
+  UCK(cudaMemcpyAsync(lab.data(), u.views[0].labels, pix[n] * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  UCK(cudaMemcpyAsync(counts.data(), u.views[0].nreg, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  UCK(cudaMemcpyAsync(counts.data() + n, u.views[0].nart, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   UCK(cudaStreamSynchronize(st));
   const double ms_mid = ms_since(t2);
-  // host: mean-boundary merge, calibration, output grid
+  // host: mean-boundary merge, calibration, output grid, one image per thread
   const auto t3 = std::chrono::steady_clock::now();
-  std::vector<double> um(double_size ? 0 : N2);
-  double* full = double_size ? ucm_out : um.data();  // the doubled grid is the caller's buffer where asked
-  ucm::mean_pb_merge(w2.data(), lab.data(), H, W, full);
-  ucm::normalize(full, N2);
-  if (!double_size) {
-    const int GW = 2 * W + 1;
-    for (int i = 0; i <= H; i++)
-      for (int j = 0; j <= W; j++)
-        ucm_out[(size_t)i * (W + 1) + j] = (i < H && j < W) ? um[(size_t)(2 * i + 2) * GW + 2 * j + 2] : 0.0;
-  }
+  ctx_parallel_for(ctx, ni, [&](int i) {
+    const size_t G2 = g2[i + 1] - g2[i];
+    std::vector<double> um(double_size ? 0 : G2);
+    double* full = double_size ? ucm_out[i] : um.data();  // the doubled grid is the caller's buffer where asked
+    ucm::mean_pb_merge(w2.data() + g2[i], lab.data() + pix[i], H[i], W[i], full);
+    ucm::normalize(full, G2);
+    if (!double_size) {
+      const int GW = 2 * W[i] + 1;
+      double* o = ucm_out[i];
+      for (int r = 0; r <= H[i]; r++)
+        for (int c = 0; c <= W[i]; c++)
+          o[(size_t)r * (W[i] + 1) + c] = (r < H[i] && c < W[i]) ? um[(size_t)(2 * r + 2) * GW + 2 * c + 2] : 0.0;
+    }
+  });
+  const double ms_merge = ms_since(t3);
   u.H = H;
   u.W = W;
-  if (info) {
-    info->n_regions = (uint32_t)counts[0];
-    info->n_vertices = (uint32_t)fit.vx.size();
-    info->n_edges = (uint32_t)ne;
-    info->n_artefacts = (uint32_t)counts[1];
-    info->fit_ok = ok ? 1 : 0;
-    info->ms_front = ms_front;
-    info->ms_fit = ms_fit;
-    info->ms_mid = ms_mid;
-    info->ms_merge = ms_since(t3);
-    info->ms_total = ms_since(t0);
+  if (info)
+    for (size_t i = 0; i < n; i++) {
+      gpb_ucm_info& f = info[i];
+      f.n_regions = (uint32_t)counts[i];
+      f.n_vertices = (uint32_t)fit[i].vx.size();
+      f.n_edges = (uint32_t)fit[i].es.size();
+      f.n_artefacts = (uint32_t)counts[n + i];
+      f.fit_ok = ok[i] ? 1 : 0;
+      f.ms_front = ms_front;
+      f.ms_fit = n == 1 ? ms_fit : ms_fit_i[i];
+      f.ms_mid = ms_mid;
+      f.ms_merge = ms_merge;
+      f.ms_total = ms_since(t0);
+    }
+  return GPB_OK;
+}
+
+extern "C" gpb_status gpb_ucm(gpb_ctx* ctx, uint32_t width, uint32_t height, const float* orient,
+                              int orient_on_device, int double_size, double* ucm_out, gpb_ucm_info* info) {
+  return gpb_ucm_batch(ctx, 1, &width, &height, &orient, orient_on_device, double_size, &ucm_out, info);
+}
+
+extern "C" gpb_status gpb_ucm_fetch(gpb_ctx* ctx, size_t image, int what, void* host, size_t bytes) {
+  if (!ctx || !host) return GPB_ERR_ARG;
+  void*& slot = ctx_ucm_state(ctx, ucm_release);
+  UcmState* u = (UcmState*)slot;
+  if (!u || image >= u->H.size()) return GPB_ERR_ARG;
+  const int H = u->H[image], W = u->W[image];
+  const UcmScratch& v = u->views[image];
+  const size_t N = (size_t)H * W, N2 = (size_t)(2 * H + 1) * (2 * W + 1);
+  const void* src = nullptr;
+  size_t need = 0;
+  switch (what) {
+    case GPB_UCM_QUANT: src = v.q; need = N; break;
+    case GPB_UCM_ARCS: src = v.bw; need = N; break;
+    case GPB_UCM_WSWT: src = v.wswt; need = N * sizeof(float); break;
+    case GPB_UCM_WSWT2: src = v.wswt2; need = N2 * sizeof(float); break;
+    case GPB_UCM_REGIONS: src = v.labels; need = N * sizeof(int32_t); break;
+    default: return GPB_ERR_ARG;
   }
+  if (bytes < need) return GPB_ERR_ARG;
+  UCK(cudaSetDevice(ctx_device(ctx)));
+  UCK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, ctx_stream(ctx)));
+  UCK(cudaStreamSynchronize(ctx_stream(ctx)));
   return GPB_OK;
 }
 
@@ -238,27 +358,4 @@ extern "C" int32_t gpb_ucm_labels_at_scale(const double* ucm2, uint32_t width, u
     for (uint32_t j = 0; j < width; j++)
       labels[(size_t)i * width + j] = (int32_t)l2[(size_t)(2 * i + 1) * GW + 2 * j + 1] - 1;
   return (int32_t)n;
-}
-
-extern "C" gpb_status gpb_ucm_fetch(gpb_ctx* ctx, int what, void* host, size_t bytes) {
-  if (!ctx || !host) return GPB_ERR_ARG;
-  void*& slot = ctx_ucm_state(ctx, ucm_release);
-  UcmState* u = (UcmState*)slot;
-  if (!u || !u->H) return GPB_ERR_ARG;
-  const size_t N = (size_t)u->H * u->W, N2 = (size_t)(2 * u->H + 1) * (2 * u->W + 1);
-  const void* src = nullptr;
-  size_t need = 0;
-  switch (what) {
-    case GPB_UCM_QUANT: src = u->s.q; need = N; break;
-    case GPB_UCM_ARCS: src = u->s.bw; need = N; break;
-    case GPB_UCM_WSWT: src = u->s.wswt; need = N * sizeof(float); break;
-    case GPB_UCM_WSWT2: src = u->s.wswt2; need = N2 * sizeof(float); break;
-    case GPB_UCM_REGIONS: src = u->s.labels; need = N * sizeof(int32_t); break;
-    default: return GPB_ERR_ARG;
-  }
-  if (bytes < need) return GPB_ERR_ARG;
-  UCK(cudaSetDevice(ctx_device(ctx)));
-  UCK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, ctx_stream(ctx)));
-  UCK(cudaStreamSynchronize(ctx_stream(ctx)));
-  return GPB_OK;
 }

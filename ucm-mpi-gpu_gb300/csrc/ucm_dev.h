@@ -17,7 +17,7 @@ struct UcmScratch {
   uint8_t* q;          // N
   int32_t* off;        // H x 257
   uint16_t* cols;      // N
-  UcmImage* img;       // 1
+  UcmImage* img;       // this image's entry of the batch's image table
   int32_t* ws;         // N
   uint8_t* bw;         // N
   float* wswt;         // N
@@ -35,7 +35,11 @@ struct UcmScratch {
   float* wswt2;        // (2H+1)(2W+1)
 };
 
-cudaError_t ucm_front(const float* d_orient, int H, int W, UcmScratch& s, cudaStream_t st);
+// per image: max over orientations, quantisation, per-row level sort
+cudaError_t ucm_prepare(const float* d_orient, int H, int W, UcmScratch& s, cudaStream_t st);
+// all images of a batch: flooding (one CTA each) and the watershed-pixel map;
+// base is image 0's view, whose arrays start the batch's concatenated ones
+cudaError_t ucm_flood(int nimg, long long total_pix, const UcmScratch& base, cudaStream_t st);
 cudaError_t ucm_paint(const float* d_orient, int H, int W, int npaint, UcmScratch& s, cudaStream_t st);
 cudaError_t ucm_mid(int H, int W, UcmScratch& s, cudaStream_t st);
 

@@ -122,7 +122,9 @@ def _lib():
         u32, i32 = ctypes.c_uint32, ctypes.c_int32
         L.gpb_ucm.argtypes = [vp, u32, u32, vp, c, c, vp, ctypes.POINTER(UcmInfo)]
         L.gpb_ucm.restype = c
-        L.gpb_ucm_fetch.argtypes = [vp, c, vp, sz]
+        L.gpb_ucm_batch.argtypes = [vp, sz, vp, vp, vp, c, c, vp, ctypes.POINTER(UcmInfo)]
+        L.gpb_ucm_batch.restype = c
+        L.gpb_ucm_fetch.argtypes = [vp, sz, c, vp, sz]
         L.gpb_ucm_fetch.restype = c
         L.gpb_ucm_fit_contours.argtypes = [vp, u32, u32, i32, i32, i32, vp, vp, vp, vp, vp]
         L.gpb_ucm_fit_contours.restype = i32
@@ -259,16 +261,33 @@ class Context:
         info = UcmInfo()
         _check(_lib().gpb_ucm(self._h, W, H, ptr, on_dev, 1 if double_size else 0, out.ctypes.data,
                               ctypes.byref(info)), "gpb_ucm")
-        self.last_ucm_shape = (H, W)
+        self.last_ucm_shapes = [(H, W)]
         return out, info.as_dict()
 
-    def ucm_fetch(self, what):
-        """an intermediate of the last ucm call (UCM_* names)"""
-        H, W = self.last_ucm_shape
+    def ucm_batch(self, orients, double_size=True):
+        """Contours2Ucm of several images in one call: ``orients`` a list of
+        (8, H, W) host arrays.  Returns a list of (map, info dict)."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in orients]
+        n = len(arrs)
+        ws = np.array([a.shape[2] for a in arrs], np.uint32)
+        hs = np.array([a.shape[1] for a in arrs], np.uint32)
+        outs = [np.empty((2 * h + 1, 2 * w + 1) if double_size else (h + 1, w + 1), np.float64)
+                for h, w in zip(hs, ws)]
+        ptr_in = (ctypes.c_void_p * n)(*[a.ctypes.data for a in arrs])
+        ptr_out = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+        infos = (UcmInfo * n)()
+        _check(_lib().gpb_ucm_batch(self._h, n, ws.ctypes.data, hs.ctypes.data, ptr_in, 0, 1 if double_size else 0,
+                                    ptr_out, infos), "gpb_ucm_batch")
+        self.last_ucm_shapes = [(int(h), int(w)) for h, w in zip(hs, ws)]
+        return [(o, infos[i].as_dict()) for i, o in enumerate(outs)]
+
+    def ucm_fetch(self, what, image=0):
+        """an intermediate of image ``image`` of the last ucm call (UCM_* names)"""
+        H, W = self.last_ucm_shapes[image]
         shape, dt = {UCM_QUANT: ((H, W), np.uint8), UCM_ARCS: ((H, W), np.uint8), UCM_WSWT: ((H, W), np.float32),
                      UCM_WSWT2: ((2 * H + 1, 2 * W + 1), np.float32), UCM_REGIONS: ((H, W), np.int32)}[what]
         out = np.empty(shape, dt)
-        _check(_lib().gpb_ucm_fetch(self._h, what, out.ctypes.data, out.nbytes), "gpb_ucm_fetch")
+        _check(_lib().gpb_ucm_fetch(self._h, image, what, out.ctypes.data, out.nbytes), "gpb_ucm_fetch")
         return out
 
     def stats(self):
