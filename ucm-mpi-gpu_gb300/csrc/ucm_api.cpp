@@ -148,13 +148,13 @@ extern "C" gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widt
                                     const float* const* orient, int orient_on_device, int double_size,
                                     double* const* ucm_out, gpb_ucm_info* info) {
   if (!ctx || n == 0 || n > 65535 || !widths || !heights || !orient || !ucm_out) return GPB_ERR_ARG;
-  size_t total4 = 0;
+  size_t total2 = 0;
   for (size_t i = 0; i < n; i++) {
     const uint32_t w = widths[i], h = heights[i];
     if (!orient[i] || !ucm_out[i] || w < 2 || h < 2 || w > 65535 || h > 65535) return GPB_ERR_ARG;
-    total4 += 4ull * w * h;
+    total2 += (2ull * h + 1) * (2ull * w + 1);
   }
-  if (total4 >= (1ull << 31)) return GPB_ERR_ARG;  // int32 indices of the doubled grids
+  if (total2 >= (1ull << 31)) return GPB_ERR_ARG;  // int32 indices of the doubled grids
   const auto t0 = std::chrono::steady_clock::now();
   const int ni = (int)n;
   std::vector<int> H(n), W(n);
