@@ -649,9 +649,10 @@ namespace {
 // copy in each region's neighbour map; both copies are always updated together).
 struct Pair {
   double energy = 0, total = 0, length = 0;
-  double pushed = -1.0;  // energy and first region of the pair's last queue entry
+  double pushed = -1.0;      // energy and first region of the pair's last queue entry
+  double raise = -INFINITY;  // pending raise of the boundary list
   int first = -1;
-  int list = -1;         // the pair's boundary coordinates
+  int head = -1, tail = -1;  // the pair's boundary coordinates: a linked list of nodes
 };
 
 // open-addressing map from an unordered region pair to its Pair index
@@ -718,14 +719,13 @@ struct Entry {
 // strengths; part: H x W region ids 0..n-1 (negative ids are skipped).
 //
 // The reference sums each pair's boundary strengths in column-major order
-// of the coordinates; each pair's list is sorted into that order first.
+// of the coordinates; the grid is walked in that order here.
 //
 // The reference walks the son's whole boundary on every merge, raising the
-// map to the merge's saliency.  Here each pair of regions keeps one list of
-// its boundary coordinates with a pending raise: the son-father list takes
-// the saliency when it closes, the son's other lists take it as a pending
-// raise and are joined to the father's (the shorter list, raised, into the
-// longer).  With saliencies that never decrease -- the reference stops
+// map to the merge's saliency.  Here each pair of regions keeps one linked
+// list of its boundary coordinates: the son-father list takes the saliency
+// when it closes, the son's other lists are joined to the father's in O(1).
+// With saliencies that never decrease -- the reference stops
 // being defined otherwise: it frees its arrays and carries on -- every
 // coordinate ends at the saliency of the merge that joins its two sides,
 // as there.
@@ -746,56 +746,95 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
   std::vector<int> up(n);  // union-find; a root is a live region, its id the father's
   for (int c = 0; c < n; c++) up[c] = c;
   std::vector<Pair> P;
-  PairTable T((size_t)n * 4);
-  std::vector<std::vector<int32_t>> lists;
-  std::vector<double> raise;
+  P.reserve((size_t)n * 8);
+  PairTable T((size_t)n * 8);
+  // each pair's boundary coordinates as a linked list of nodes (coordinate,
+  // next); lists are joined in O(1) when their pairs join
+  std::vector<int32_t> node_coord, node_next;
+  node_coord.reserve((size_t)H * W);
+  node_next.reserve((size_t)H * W);
   std::vector<std::vector<std::pair<int, int>>> nb(n), pending(n);  // (neighbour, pair index)
-  // boundary coordinates, (odd, even) between horizontal neighbours and
-  // (even, odd) between vertical ones, gathered row by row and then put in
-  // the reference's column-major order before summing
-  int last_a[2] = {-1, -1}, last_b[2] = {-1, -1}, last_p[2] = {-1, -1};  // runs repeat a pair
-  for (int x = 0; x < H; x++)
-    for (int y = 0; y < W; y++) {
-      const int b = part[(size_t)x * W + y];
-      for (int side = 0; side < 2; side++) {
-        if (side == 0 ? y == 0 : x == 0) continue;
-        const int a = side == 0 ? part[(size_t)x * W + y - 1] : part[(size_t)(x - 1) * W + y];
-        if (a < 0 || b < 0 || a == b) continue;
-        const size_t np = P.size();
-        int pi;
-        if (a == last_a[side] && b == last_b[side]) {
-          pi = last_p[side];
-        } else {
-          pi = T.find(a, b, &P);
-          last_a[side] = a;
-          last_b[side] = b;
-          last_p[side] = pi;
-        }
-        if (P.size() != np) {
-          P[pi].list = (int)lists.size();
-          lists.emplace_back();
-          raise.push_back(-INFINITY);
-          nb[a].push_back({b, pi});
-          nb[b].push_back({a, pi});
-        }
-        const int gr = side == 0 ? 2 * x + 1 : 2 * x, gc = side == 0 ? 2 * y : 2 * y + 1;
-        lists[P[pi].list].push_back(gr * GW + gc);
+  // Boundary coordinates in the reference's column-major order, so that
+  // each pair's sum runs in that order: grid column 2y holds the (odd, even)
+  // coordinates between horizontal neighbours (x, y-1), (x, y); grid column
+  // 2y+1 the (even, odd) ones between vertical neighbours (x-1, y), (x, y).
+  // A transposed copy of the labels makes the walk sequential.
+  std::vector<int32_t> tr((size_t)H * W);
+  for (int x0 = 0; x0 < H; x0 += 32)
+    for (int y0 = 0; y0 < W; y0 += 32)
+      for (int x = x0; x < std::min(H, x0 + 32); x++)
+        for (int y = y0; y < std::min(W, y0 + 32); y++) tr[(size_t)y * H + x] = part[(size_t)x * W + y];
+  int last_a = -1, last_b = -1, last_p = -1;  // runs repeat a pair
+  auto add = [&](int a, int b, int32_t coord) {
+    if (a < 0 || b < 0 || a == b) return;
+    int pi;
+    if (a == last_a && b == last_b) {
+      pi = last_p;
+    } else {
+      const size_t np = P.size();
+      pi = T.find(a, b, &P);
+      if (P.size() != np) {
+        nb[a].push_back({b, pi});
+        nb[b].push_back({a, pi});
       }
+      last_a = a;
+      last_b = b;
+      last_p = pi;
     }
-  for (Pair& pr : P) {
-    std::vector<int32_t>& l = lists[pr.list];
-    std::sort(l.begin(), l.end(), [&](int32_t s0, int32_t s1) {
-      const int c0 = s0 % GW, c1 = s1 % GW;
-      return c0 != c1 ? c0 < c1 : s0 < s1;
-    });
-    for (int32_t c : l) {
-      pr.total += (double)lb[c];
-      pr.length += 1.0;
+    Pair& pr = P[pi];
+    const int32_t nd = (int32_t)node_coord.size();
+    node_coord.push_back(coord);
+    node_next.push_back(-1);
+    if (pr.tail < 0) pr.head = nd;
+    else node_next[pr.tail] = nd;
+    pr.tail = nd;
+    pr.total += (double)lb[coord];
+    pr.length += 1.0;
+  };
+  for (int y = 0; y < W; y++) {
+    const int32_t* cur = tr.data() + (size_t)y * H;
+    if (y > 0) {
+      const int32_t* left = cur - H;
+      for (int x = 0; x < H; x++) add(left[x], cur[x], (2 * x + 1) * GW + 2 * y);
     }
+    for (int x = 1; x < H; x++) add(cur[x - 1], cur[x], (2 * x) * GW + 2 * y + 1);
   }
-  std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> q;
+  std::vector<int32_t>().swap(tr);
+  // a 4-ary min-heap in the reference's (energy, region1, region2) order
+  std::vector<Entry> heap;
+  heap.reserve(P.size() * 2);
+  auto before = [](const Entry& a, const Entry& b) { return b > a; };
+  auto heap_push = [&](const Entry& e) {
+    size_t i = heap.size();
+    heap.push_back(e);
+    while (i > 0) {
+      const size_t par = (i - 1) / 4;
+      if (!before(heap[i], heap[par])) break;
+      std::swap(heap[i], heap[par]);
+      i = par;
+    }
+  };
+  auto heap_pop = [&]() {
+    const Entry top = heap[0];
+    heap[0] = heap.back();
+    heap.pop_back();
+    const size_t sz = heap.size();
+    size_t i = 0;
+    for (;;) {
+      const size_t c0 = 4 * i + 1;
+      if (c0 >= sz) break;
+      size_t best = c0;
+      const size_t ce = std::min(c0 + 4, sz);
+      for (size_t c = c0 + 1; c < ce; c++)
+        if (before(heap[c], heap[best])) best = c;
+      if (!before(heap[best], heap[i])) break;
+      std::swap(heap[i], heap[best]);
+      i = best;
+    }
+    return top;
+  };
   auto push = [&](int pi, double d, int a, int b) {  // entry (d, a, b); b is the region that pushes
-    q.push({d, a, b, pi});
+    heap_push({d, a, b, pi});
     P[pi].pushed = d;
     P[pi].first = a;
     pending[a].push_back({b, pi});
@@ -807,22 +846,21 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
         pr.energy = pr.total / pr.length;
         push(kp.second, pr.energy, c, kp.first);
       }
-  auto flush = [&](int l, double extra) {
-    const double r = std::max(raise[l], extra);
-    for (int32_t c : lists[l])
-      if (ucm[c] < r) ucm[c] = r;
-    std::vector<int32_t>().swap(lists[l]);
+  auto flush = [&](Pair& pr, double extra) {
+    const double r = std::max(pr.raise, extra);
+    for (int32_t k = pr.head; k >= 0; k = node_next[k])
+      if (ucm[node_coord[k]] < r) ucm[node_coord[k]] = r;
+    pr.head = pr.tail = -1;
   };
   std::vector<std::pair<int, int>> touched;
-  while (!q.empty()) {
-    const Entry m = q.top();
-    q.pop();
+  while (!heap.empty()) {
+    const Entry m = heap_pop();
     if (up[m.r1] != m.r1 || up[m.r2] != m.r2) continue;
     const int ci = m.pair;  // both regions live, so the pair is the one pushed
     if (m.energy != P[ci].energy) continue;
     const double saliency = P[ci].total / P[ci].length;
     const int son = std::min(m.r1, m.r2), father = std::max(m.r1, m.r2);
-    if (P[ci].list >= 0) flush(P[ci].list, saliency);  // the son-father boundary becomes interior
+    flush(P[ci], saliency);  // the son-father boundary becomes interior
     up[son] = father;
     // the son's live neighbours other than the father join the father's
     touched.clear();
@@ -838,18 +876,15 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
       Pair &s = P[si], &f = P[fi];
       f.total += s.total;
       f.length += s.length;
-      raise[s.list] = std::max(raise[s.list], saliency);
-      if (f.list < 0) {
-        f.list = s.list;
-      } else {
-        int big = f.list, small = s.list;
-        if (lists[small].size() > lists[big].size()) std::swap(big, small);
-        const double r = raise[small];
-        for (int32_t c : lists[small])
-          if (ucm[c] < r) ucm[c] = r;
-        lists[big].insert(lists[big].end(), lists[small].begin(), lists[small].end());
-        std::vector<int32_t>().swap(lists[small]);
-        f.list = big;
+      // the son's side is raised to this saliency; with saliencies that
+      // never decrease only the raise at closing shows, so lists join as
+      // they are and keep the larger pending raise
+      if (s.head >= 0) {
+        if (f.head < 0) f.head = s.head;
+        else node_next[f.tail] = s.head;
+        f.tail = s.tail;
+        f.raise = std::max(f.raise, std::max(s.raise, saliency));
+        s.head = s.tail = -1;
       }
       touched.push_back({k, fi});
     }
@@ -873,8 +908,8 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
       v.resize(w);
     }
   }
-  for (size_t l = 0; l < lists.size(); l++)  // boundaries never closed (a split adjacency graph)
-    if (!lists[l].empty()) flush((int)l, -INFINITY);
+  for (Pair& pr : P)  // boundaries never closed (a split adjacency graph)
+    if (pr.head >= 0) flush(pr, -INFINITY);
   // CompleteContourMap: every even-even grid point takes the largest of its
   // four neighbours (starting from 0)
   for (int x = 0; x < GH; x += 2)
