@@ -50,6 +50,8 @@ CASES = {
     "gpb48x64": lambda: gpb_planes(48, 64, 5),
     "tiny5x7": lambda: smooth_planes(5, 7, 11, 0.7),
     "flat32": lambda: np.full((8, 32, 32), 0.25, np.float32),
+    "noise2x3": lambda: np.random.default_rng(23).random((8, 2, 3)).astype(np.float32),
+    "noise4x9": lambda: np.random.default_rng(49).random((8, 4, 9)).astype(np.float32),
 }
 
 

@@ -14,7 +14,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import ucm_oracle as uo  # noqa: E402
 
 GOLD = os.path.join(ROOT, "tests", "golden", "ucm_cases.npz")
-CASES = ["rand40x50", "rand80x64", "gpb48x64", "tiny5x7", "flat32"]
+CASES = ["rand40x50", "rand80x64", "gpb48x64", "tiny5x7", "flat32", "noise2x3", "noise4x9"]
 UCM_TOL = 1e-12  # calibration goes through exp(); numpy's and libm's may differ in the last bit
 
 
