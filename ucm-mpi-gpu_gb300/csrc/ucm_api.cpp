@@ -201,9 +201,11 @@ extern "C" gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widt
   std::vector<std::vector<int32_t>> ppix(n);
   std::vector<std::vector<uint8_t>> pori(n);
   std::vector<double> ms_fit_i(n);
+  const ucm::ParFor pool = [&](int k, const std::function<void(int)>& f) { ctx_parallel_for(ctx, k, f); };
   ctx_parallel_for(ctx, ni, [&](int i) {
     const auto ti = std::chrono::steady_clock::now();
-    ok[i] = ucm::fit_contours(bw.data() + pix[i], H[i], W[i], fit[i]);
+    // one image alone uses the pool inside its contour fitting instead
+    ok[i] = ucm::fit_contours(bw.data() + pix[i], H[i], W[i], fit[i], n == 1 ? &pool : nullptr);
     const ucm::FitResult& f = fit[i];
     const int ne = (int)f.es.size();
     ppix[i].reserve(f.px.size() + 2 * ne);

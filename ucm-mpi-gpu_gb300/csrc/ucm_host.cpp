@@ -135,12 +135,13 @@ struct Edge {
 
 class Contours {
  public:
-  Contours(const uint8_t* bw, int H, int W) : H_(H), W_(W) { build(bw); }
+  Contours(const uint8_t* bw, int H, int W, const ParFor* par) : H_(H), W_(W), par_(par) { build(bw); }
 
   void subdivide_local();
   bool subdivide_global();  // false where the reference throws
 
   int H_, W_;
+  const ParFor* par_;  // host pool for the crossing tests, or null
   std::vector<Vert> vert;
   std::vector<Edge> edge;
 
@@ -497,92 +498,106 @@ bool Contours::subdivide_global() {
     }
     auto cell_begin = [&](size_t c) { return cell_items.data() + cstart[c]; };
     auto cell_end = [&](size_t c) { return cell_items.data() + cstart[c + 1]; };
-    std::vector<uint8_t> mark(ne, 0);
-    bool found = false;
-    // (a) a vertex inside a chord's interior: every such chord is split
-    for (size_t v = 0; v < nv; v++) {
-      const i64 px = vert[v].x, py = vert[v].y;
-      const size_t cv = (size_t)(px / CS) * GY + py / CS;
-      for (const int* it = cell_begin(cv); it != cell_end(cv); ++it) {
-        const int e = *it;
-        const int a = edge[e].vs, b = edge[e].ve;
-        if (a == (int)v || b == (int)v) continue;
-        const i64 ax = vert[a].x, ay = vert[a].y, bx = vert[b].x, by = vert[b].y;
-        if (orient(ax, ay, bx, by, px, py) != 0) continue;
-        const bool lo_a = lex_less(ax, ay, bx, by);
-        const i64 lx = lo_a ? ax : bx, ly = lo_a ? ay : by, ux = lo_a ? bx : ax, uy = lo_a ? by : ay;
-        if (lex_less(lx, ly, px, py) && lex_less(px, py, ux, uy)) {
-          mark[e] = 1;
-          found = true;
-        }
-      }
-    }
-    // (b) two chords crossing at a point that is no vertex: the one whose
-    // contour comes nearer the other's chord is kept, the other split
-    std::vector<std::pair<int, int>> pairs;
-    for (int cx = 0; cx < GX; cx++)
-      for (int cy = 0; cy < GY; cy++) {
-        const int* c = cell_begin((size_t)cx * GY + cy);
-        const size_t csz = (size_t)(cell_end((size_t)cx * GY + cy) - c);
-        for (size_t i = 0; i < csz; i++)
-          for (size_t j = i + 1; j < csz; j++) {
-            const Vert &a0 = vert[edge[c[i]].vs], &a1 = vert[edge[c[i]].ve];
-            const Vert &b0 = vert[edge[c[j]].vs], &b1 = vert[edge[c[j]].ve];
-            const int lx = std::max(std::min(a0.x, a1.x), std::min(b0.x, b1.x));
-            const int ly = std::max(std::min(a0.y, a1.y), std::min(b0.y, b1.y));
-            const int hx = std::min(std::max(a0.x, a1.x), std::max(b0.x, b1.x));
-            const int hy = std::min(std::max(a0.y, a1.y), std::max(b0.y, b1.y));
-            if (lx > hx || ly > hy || lx / CS != cx || ly / CS != cy) continue;  // no overlap, or not its first cell
-            pairs.push_back({std::min(c[i], c[j]), std::max(c[i], c[j])});
+    // the marks form a set, so slices of the vertices and of the cell rows
+    // are scanned independently (on the host pool when one is given)
+    const int nt = par_ ? 16 : 1;
+    std::vector<std::vector<uint8_t>> marks(nt, std::vector<uint8_t>(ne, 0));
+    std::vector<char> founds(nt, 0);
+    auto scan = [&](int t) {
+      std::vector<uint8_t>& mark = marks[t];
+      char found = 0;
+      // (a) a vertex inside a chord's interior: every such chord is split
+      for (size_t v = nv * t / nt; v < nv * (t + 1) / nt; v++) {
+        const i64 px = vert[v].x, py = vert[v].y;
+        const size_t cv = (size_t)(px / CS) * GY + py / CS;
+        for (const int* it = cell_begin(cv); it != cell_end(cv); ++it) {
+          const int e = *it;
+          const int a = edge[e].vs, b = edge[e].ve;
+          if (a == (int)v || b == (int)v) continue;
+          const i64 ax = vert[a].x, ay = vert[a].y, bx = vert[b].x, by = vert[b].y;
+          if (orient(ax, ay, bx, by, px, py) != 0) continue;
+          const bool lo_a = lex_less(ax, ay, bx, by);
+          const i64 lx = lo_a ? ax : bx, ly = lo_a ? ay : by, ux = lo_a ? bx : ax, uy = lo_a ? by : ay;
+          if (lex_less(lx, ly, px, py) && lex_less(px, py, ux, uy)) {
+            mark[e] = 1;
+            found = 1;
           }
-      }
-    for (const auto& pr : pairs) {
-      const int s = pr.first, t = pr.second;
-      const i64 ax = vert[edge[s].vs].x, ay = vert[edge[s].vs].y, bx = vert[edge[s].ve].x, by = vert[edge[s].ve].y;
-      const i64 cx = vert[edge[t].vs].x, cy = vert[edge[t].vs].y, dx = vert[edge[t].ve].x, dy = vert[edge[t].ve].y;
-      const int o1 = orient(ax, ay, bx, by, cx, cy), o2 = orient(ax, ay, bx, by, dx, dy);
-      const int o3 = orient(cx, cy, dx, dy, ax, ay), o4 = orient(cx, cy, dx, dy, bx, by);
-      if (!(o1 * o2 < 0 && o3 * o4 < 0)) continue;  // no proper crossing
-      // crossing point = a + (b - a) * num / den, exactly
-      const i64 den = (bx - ax) * (dy - cy) - (by - ay) * (dx - cx);
-      const i64 num = (cx - ax) * (dy - cy) - (cy - ay) * (dx - cx);
-      const i64 X = ax * den + (bx - ax) * num, Y = ay * den + (by - ay) * num;
-      if (X % den == 0 && Y % den == 0) {  // an integer crossing point: is it a vertex?
-        const i64 xi = X / den, yi = Y / den;
-        if (xi >= 0 && xi < H_ && yi >= 0 && yi < W_ && is_v_[(size_t)xi * W_ + yi]) continue;  // handled under (a)
-      }
-      found = true;
-      // order the two as the sweep does at the crossing: by the angle of
-      // the part left of the sweep line (compute_sweep_line_angle)
-      const double fx = (double)X / (double)den, fy = (double)Y / (double)den;
-      auto ang = [&](int e) {
-        const Vert &p = vert[edge[e].vs], &q = vert[edge[e].ve];
-        const Vert& lo = lex_less(p.x, p.y, q.x, q.y) ? p : q;
-        return atan2(fx - lo.x, fy - lo.y);
-      };
-      const double a0 = ang(s), a1 = ang(t);
-      int ea = s, eb = t;
-      if (a1 < a0) std::swap(ea, eb);
-      if (edge[ea].px.empty()) {
-        mark[eb] = 1;
-        continue;
-      }
-      if (edge[eb].px.empty()) {
-        mark[ea] = 1;
-        continue;
-      }
-      auto closest = [&](int e, int other) {  // find_contour_point_closest_to_segment
-        const int p = edge[other].vs, q = edge[other].ve;
-        double best = dist_seg(edge[e].px[0], p, q);
-        size_t pos = 0;
-        for (size_t n = 1; n < edge[e].px.size(); n++) {
-          const double d = dist_seg(edge[e].px[n], p, q);
-          if (d < best) pos = n, best = d;
         }
-        return dist_seg(edge[e].px[pos], p, q);
-      };
-      if (closest(ea, eb) < closest(eb, ea)) mark[eb] = 1;
-      else mark[ea] = 1;
+      }
+      // (b) two chords crossing at a point that is no vertex: the one whose
+      // contour comes nearer the other's chord is kept, the other split.
+      // A pair is tested in the cell holding the corner of its boxes' overlap.
+      for (int cx = GX * t / nt; cx < GX * (t + 1) / nt; cx++)
+        for (int cy = 0; cy < GY; cy++) {
+          const int* c = cell_begin((size_t)cx * GY + cy);
+          const size_t csz = (size_t)(cell_end((size_t)cx * GY + cy) - c);
+          for (size_t i = 0; i < csz; i++)
+            for (size_t j = i + 1; j < csz; j++) {
+              const int s = std::min(c[i], c[j]), tt = std::max(c[i], c[j]);
+              const Vert &a0 = vert[edge[s].vs], &a1 = vert[edge[s].ve];
+              const Vert &b0 = vert[edge[tt].vs], &b1 = vert[edge[tt].ve];
+              const int lx = std::max(std::min(a0.x, a1.x), std::min(b0.x, b1.x));
+              const int ly = std::max(std::min(a0.y, a1.y), std::min(b0.y, b1.y));
+              const int hx = std::min(std::max(a0.x, a1.x), std::max(b0.x, b1.x));
+              const int hy = std::min(std::max(a0.y, a1.y), std::max(b0.y, b1.y));
+              if (lx > hx || ly > hy || lx / CS != cx || ly / CS != cy) continue;
+              const i64 ax = a0.x, ay = a0.y, bx = a1.x, by = a1.y;
+              const i64 qx = b0.x, qy = b0.y, dx = b1.x, dy = b1.y;
+              const int o1 = orient(ax, ay, bx, by, qx, qy), o2 = orient(ax, ay, bx, by, dx, dy);
+              const int o3 = orient(qx, qy, dx, dy, ax, ay), o4 = orient(qx, qy, dx, dy, bx, by);
+              if (!(o1 * o2 < 0 && o3 * o4 < 0)) continue;  // no proper crossing
+              // crossing point = a + (b - a) * num / den, exactly
+              const i64 den = (bx - ax) * (dy - qy) - (by - ay) * (dx - qx);
+              const i64 num = (qx - ax) * (dy - qy) - (qy - ay) * (dx - qx);
+              const i64 X = ax * den + (bx - ax) * num, Y = ay * den + (by - ay) * num;
+              if (X % den == 0 && Y % den == 0) {  // an integer crossing point: is it a vertex?
+                const i64 xi = X / den, yi = Y / den;
+                if (xi >= 0 && xi < H_ && yi >= 0 && yi < W_ && is_v_[(size_t)xi * W_ + yi]) continue;  // under (a)
+              }
+              found = 1;
+              // order the two as the sweep does at the crossing: by the angle of
+              // the part left of the sweep line (compute_sweep_line_angle)
+              const double fx = (double)X / (double)den, fy = (double)Y / (double)den;
+              auto ang = [&](int e) {
+                const Vert &p = vert[edge[e].vs], &q = vert[edge[e].ve];
+                const Vert& lo = lex_less(p.x, p.y, q.x, q.y) ? p : q;
+                return atan2(fx - lo.x, fy - lo.y);
+              };
+              const double g0 = ang(s), g1 = ang(tt);
+              int ea = s, eb = tt;
+              if (g1 < g0) std::swap(ea, eb);
+              if (edge[ea].px.empty()) {
+                mark[eb] = 1;
+                continue;
+              }
+              if (edge[eb].px.empty()) {
+                mark[ea] = 1;
+                continue;
+              }
+              auto closest = [&](int e, int other) {  // find_contour_point_closest_to_segment
+                const int p = edge[other].vs, q = edge[other].ve;
+                double best = dist_seg(edge[e].px[0], p, q);
+                size_t pos = 0;
+                for (size_t n = 1; n < edge[e].px.size(); n++) {
+                  const double d = dist_seg(edge[e].px[n], p, q);
+                  if (d < best) pos = n, best = d;
+                }
+                return dist_seg(edge[e].px[pos], p, q);
+              };
+              if (closest(ea, eb) < closest(eb, ea)) mark[eb] = 1;
+              else mark[ea] = 1;
+            }
+        }
+      founds[t] = found;
+    };
+    if (par_) (*par_)(nt, scan);
+    else scan(0);
+    bool found = false;
+    std::vector<uint8_t>& mark = marks[0];
+    for (int t = 0; t < nt; t++) {
+      found = found || founds[t];
+      if (t)
+        for (size_t e = 0; e < ne; e++) mark[e] |= marks[t][e];
     }
     if (!found) break;
     for (size_t e = 0; e < ne; e++) {
@@ -598,8 +613,8 @@ bool Contours::subdivide_global() {
 // the non-completion edges and their interior pixels.  Returns false where
 // the reference's subdivision throws, in which case MexContourSides returns
 // no contours and nothing is painted.
-bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out) {
-  Contours c(bw, H, W);
+bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out, const ParFor* par) {
+  Contours c(bw, H, W, par);
   c.subdivide_local();
   const bool ok = c.subdivide_global();
   out.vx.clear();

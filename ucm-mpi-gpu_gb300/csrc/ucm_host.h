@@ -4,6 +4,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <functional>
 #include <vector>
 
 namespace gpb {
@@ -16,7 +17,9 @@ struct FitResult {
 };
 
 uint32_t components8(const uint8_t* bw, int H, int W, std::vector<uint32_t>& lab);
-bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out);
+// runs f(0..n-1), possibly on several threads
+using ParFor = std::function<void(int, const std::function<void(int)>&)>;
+bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out, const ParFor* par = nullptr);
 int edge_orientation(int x1, int y1, int x2, int y2);
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm);
 void mean_pb_merge(const float* lb, const int32_t* part, int H, int W, double* ucm);
