@@ -139,11 +139,14 @@ __global__ void __launch_bounds__(32) k_ws_rowsort(const uint8_t* __restrict__ q
 // One CTA of 1024 threads per image; warp w owns grey levels w, w + 32, ...
 // At step t a warp takes, level by level, the row t - 2l of its level l
 // and walks that row's pixels of level l in column order, 32 at a time:
-// every lane gathers the labels of its pixel's 8 neighbours at once (the
-// pixel to its left is still unlabelled when it is the previous lane's,
-// so it is left out), then runs of adjacent pixels are resolved lane by
-// lane.  ws is -1 (not reached), 0 (watershed pixel) or a region label
-// (> 0): a new region takes the label 1 + its pixel index.
+// every lane gathers the labels of its pixel's 8 neighbours at once, then
+// runs of adjacent pixels are resolved lane by lane, and most lanes settle
+// without waiting because their label cannot depend on the left one.  The
+// next 32 pixels' neighbours are loaded before the current ones resolve;
+// the one of them that the current 32 may still write (the left neighbour
+// of the next first pixel) is taken from the current last pixel instead.
+// ws is -1 (not reached), 0 (watershed pixel) or a region label (> 0): a
+// new region takes the label 1 + its pixel index.
 __global__ void __launch_bounds__(1024) k_ws_flood(const UcmImage* __restrict__ imgs, const int32_t* __restrict__ off,
                                                    const uint16_t* __restrict__ cols, int32_t* __restrict__ ws) {
   const UcmImage I = imgs[blockIdx.x];
@@ -153,47 +156,72 @@ __global__ void __launch_bounds__(1024) k_ws_flood(const UcmImage* __restrict__ 
   const uint16_t* C = cols + I.pix;
   for (long long p = threadIdx.x; p < (long long)H * W; p += blockDim.x) L[p] = -1;
   __syncthreads();
+  constexpr int kLeft = 3;  // index of (0, -1) in the neighbour order below
   const int steps = 2 * 255 + H;
   for (int t = 0; t < steps; t++) {
     for (int lvl = warp; lvl < 256; lvl += 32) {
       const int x = t - 2 * lvl;
       if (x < 0 || x >= H) continue;
       const int b = O[x * 257 + lvl], e = O[x * 257 + lvl + 1];
+      if (b >= e) continue;
+      // the labels around the k-th pixel of the segment (-1 outside the image or the segment)
+      auto gather = [&](int k, int& y, int (&nbv)[8]) {
+        y = k < e ? (int)C[(size_t)x * W + k] : -4;
+        int idx = 0;
+        for (int i = -1; i <= 1; i++)
+          for (int j = -1; j <= 1; j++) {
+            if (i == 0 && j == 0) continue;
+            const int xi = x + i, yj = y + j;
+            nbv[idx++] = (k < e && xi >= 0 && xi < H && yj >= 0 && yj < W) ? L[(size_t)xi * W + yj] : -1;
+          }
+      };
+      int y, nbv[8];
+      gather(b + lane, y, nbv);
+      int carry = -1, ylast = -10;  // final label and column of the previous chunk's last pixel
       for (int k0 = b; k0 < e; k0 += 32) {
         const int k = k0 + lane;
         const bool in = k < e;
-        const int y = in ? C[(size_t)x * W + k] : -4;
+        int yn, nbn[8];
+        gather(k0 + 32 + lane, yn, nbn);  // the next chunk, in flight while this one resolves
         const int yl = __shfl_up_sync(0xffffffffu, y, 1);
-        const bool dep = in && lane > 0 && yl == y - 1;  // its left neighbour is the previous lane's pixel
+        const bool cross = in && lane == 0 && y - 1 == ylast;          // left pixel in the previous chunk
+        const bool dep = in && (cross || (lane > 0 && yl == y - 1));  // left pixel is this level's, unresolved here
         int s = -1;  // -1: no labelled neighbour, 0: two different labels, else the one label
-        if (in) {
-          for (int i = -1; i <= 1; i++) {
-            const int xi = x + i;
-            if (xi < 0 || xi >= H) continue;
-            for (int j = -1; j <= 1; j++) {
-              const int yj = y + j;
-              if ((i == 0 && j == 0) || yj < 0 || yj >= W) continue;
-              const int v = L[(size_t)xi * W + yj];
-              if (v > 0) s = (s == -1) ? v : (v != s ? 0 : s);
-            }
-          }
+        for (int idx = 0; idx < 8; idx++) {
+          if (idx == kLeft && dep) continue;
+          const int v = nbv[idx];
+          if (v > 0) s = (s == -1) ? v : (v != s ? 0 : s);
         }
         const int sl = __shfl_up_sync(0xffffffffu, s, 1);
         const int mine = x * W + y + 1;
-        // final without the left lane: no dependence, a conflict already, or
-        // a label the left pixel can only repeat or have lost to a conflict
-        int done = !in || !dep || s == 0 || (s > 0 && (sl == s || sl == 0));
-        int val = !dep ? (s >= 0 ? s : mine) : s;
+        auto after = [&](int pv) {  // this pixel's label given the left pixel's
+          return (s == -1) ? (pv > 0 ? pv : mine) : ((pv > 0 && pv != s) ? 0 : s);
+        };
+        int done, val;
+        if (cross) {
+          val = after(carry);
+          done = 1;
+        } else {
+          // final without the left lane: no dependence, a conflict already, or
+          // a label the left pixel can only repeat or have lost to a conflict
+          done = !in || !dep || s == 0 || (s > 0 && (sl == s || sl == 0));
+          val = !dep ? (s >= 0 ? s : mine) : s;
+        }
         while (!__all_sync(0xffffffffu, done)) {
           const int pv = __shfl_up_sync(0xffffffffu, val, 1);
           const int pd = __shfl_up_sync(0xffffffffu, done, 1);
           if (!done && pd) {
-            val = (s == -1) ? (pv > 0 ? pv : mine) : ((pv > 0 && pv != s) ? 0 : s);
+            val = after(pv);
             done = 1;
           }
         }
         if (in) L[(size_t)x * W + y] = val;
+        const int last = min(31, e - 1 - k0);
+        carry = __shfl_sync(0xffffffffu, val, last);
+        ylast = __shfl_sync(0xffffffffu, y, last);
         __syncwarp();
+        y = yn;
+        for (int idx = 0; idx < 8; idx++) nbv[idx] = nbn[idx];
       }
     }
     __syncthreads();
