@@ -294,7 +294,8 @@ def run_gpu(args):
         serial_ms = (time.perf_counter() - t0) * 1e3
         ucm = {"image": "the step's 1024 x 1024 stitched gPb orientation planes", "ms": ums,
                "mpix_s": 1024 * 1024 / 1e6 / (ums / 1e3), "steps": args.ucm_steps,
-               "stages_ms": {k: info[k] for k in ("ms_front", "ms_fit", "ms_mid", "ms_merge")},
+               "ms_min": float(np.min(uts)),
+               "stages_ms": {k: info[k] for k in ("ms_front", "ms_fit", "ms_mid", "ms_merge", "ms_total")},
                "regions": info["n_regions"], "edges": info["n_edges"], "artefacts": info["n_artefacts"],
                "pieces_4x4_256": {"batched_ms": batch_ms, "single_calls_ms": serial_ms,
                                   "note": "host planes in, maps out; one gpb_ucm_batch call vs 16 gpb_ucm calls"}}
