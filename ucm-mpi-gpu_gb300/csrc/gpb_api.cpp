@@ -110,6 +110,7 @@ struct Buf {
   float* blk[4] = {nullptr, nullptr, nullptr, nullptr}; size_t c_blk[4] = {0, 0, 0, 0};
   double* bpart = nullptr; size_t c_bpart = 0;
   double* bgram = nullptr; size_t c_bgram = 0;
+  double* bgram2 = nullptr; size_t c_bgram2 = 0;
   double* bmat = nullptr; size_t c_bmat = 0;
   double* btheta = nullptr; size_t c_btheta = 0;
   double* bres = nullptr; size_t c_bres = 0;
@@ -454,7 +455,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
                   b.part, b.hbuf, b.T, b.Y, b.beta2, b.counter, b.active, b.decision, b.nkeep, b.evals,
                   b.mm, b.spb, b.gpbo, b.nmax, b.orient, b.patches, b.work_tex, b.work_cue, b.work16, b.work_blk,
                   b.tiles, b.tile_begin, b.tile_count, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
-                  b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bmat, b.btheta, b.bres,
+                  b.blk[0], b.blk[1], b.blk[2], b.blk[3], b.bpart, b.bgram, b.bgram2, b.bmat, b.btheta, b.bres,
                   b.bcoef, b.bdone, b.cpatches, b.ctiles, b.ctile_begin, b.ctile_count, b.cwork_blk,
                   b.cwork16, b.cwc, b.cdeg, b.cdis, b.cblk[0], b.cblk[1], b.cblk[2], b.cblk[3], b.afull, b.berr, b.work_act, b.stitch, b.spcount, b.spcsum};
   for (void* q : ptrs)
@@ -651,6 +652,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     es.push_back(grow(b.berr, b.c_berr, 1));
     es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
+    es.push_back(grow(b.bgram2, b.c_bgram2, np * kBlk * kBlk));
     es.push_back(grow(b.bmat, b.c_bmat, np * kBlk * kBlk));
     es.push_back(grow(b.btheta, b.c_btheta, np * kBlk));
     es.push_back(grow(b.bres, b.c_bres, np * kBlk));
@@ -939,10 +941,10 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   a.theta = b.btheta;
   const size_t BB = (size_t)kBlk * kBlk;
   std::vector<int> active(np, 1), done(np, 0);
-  // G, M (32 x 32 per patch), theta, res and the filter coefficients live in
-  // one pinned block, so their copies are direct DMA
+  // G, M, G2 (32 x 32 per patch), theta, res and the filter coefficients
+  // live in one pinned block, so their copies are direct DMA
   const size_t nG = np * BB, nT = np * (size_t)kBlk, nC = np * (size_t)kMaxCheb;
-  const size_t need = (2 * nG + 2 * nT) * sizeof(double) + nC * sizeof(float3);
+  const size_t need = (3 * nG + 2 * nT) * sizeof(double) + nC * sizeof(float3);
   if (ctx->c_hsmall < need) {
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     ctx->h_small = nullptr;
@@ -959,7 +961,8 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     double* begin() { return p; }
   };
   double* hb = (double*)ctx->h_small;
-  HostArr G{hb, nG}, M{hb + nG, nG}, theta{hb + 2 * nG, nT}, res{hb + 2 * nG + nT, nT};
+  HostArr G{hb, nG}, M{hb + nG, nG}, theta{hb + 2 * nG, nT}, res{hb + 2 * nG + nT, nT},
+      G2{hb + 2 * nG + 2 * nT, nG};
   for (size_t i = 0; i < nT; i++) theta[i] = 0.0;
   struct CoefArr {
     float3* p;
@@ -967,7 +970,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     float3& operator[](size_t i) { return p[i]; }
     float3* data() { return p; }
     size_t size() const { return n; }
-  } coef{(float3*)(hb + 2 * nG + 2 * nT), nC};
+  } coef{(float3*)(hb + 3 * nG + 2 * nT), nC};
   std::vector<float> evals((size_t)np * nev, 0.f);
   std::vector<long> mv(np, 0);
   // stagnation: the best worst-residual of each patch and the outer
@@ -992,39 +995,61 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     for (int i = 0; i < np; i++) coef[(size_t)i * kMaxCheb] = make_float3(1.f, 0.f, 0.f);
     return cudaMemcpyAsync(b.bcoef, coef.data(), coef.size() * sizeof(float3), cudaMemcpyHostToDevice, s);
   };
-  // orthonormalise F twice, then Rayleigh-Ritz on span(F); AF receives A F
+  // orthonormalise F (symmetric orthonormalisation), then Rayleigh-Ritz on
+  // span(F) in the metric of F's Gram matrix, which folds a second
+  // orthonormalisation into the same host step; AF receives A F.
   // comp: compensated Rayleigh-Ritz product and rotation (see cf_step_t, cf_rotate)
   auto rr = [&](float* F, float* AF, bool comp) -> gpb_status {
-    for (int pass = 0; pass < 2; pass++) {
-      CK(cf_launch_gram(a, nt, F, F, b.bgram, s));
-      CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      ctx->host_pool().run(np, [&](int i) {
-        if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
-      });
-      if (ctx->trace && active[0])
-        fprintf(stderr, "[gpb] gram pass %d patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", pass, G[0],
-                G[kBlk + 1], G[BB - 1], M[0]);
-      CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
-      CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
-      ctx->launches += 2;
-    }
-    CK(upload_unit());
-    CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s, comp));
-    CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
+    CK(cf_launch_gram(a, nt, F, F, b.bgram, s));
     CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    ctx->launches += 2;
+    ctx->host_pool().run(np, [&](int i) {
+      if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
+    });
+    if (ctx->trace && active[0])
+      fprintf(stderr, "[gpb] gram patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", G[0], G[kBlk + 1], G[BB - 1],
+              M[0]);
+    CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
+    CK(upload_unit());
+    CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s, comp));
+    CK(cf_launch_gram(a, nt, F, F, b.bgram2, s));
+    CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
+    CK(cudaMemcpyAsync(G2.data(), b.bgram2, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ctx->launches += 5;
     ctx->host_pool().run(np, [&](int i) {
       if (!active[i]) return;
       mv[i] += kBlk;
-      std::vector<double> H(BB), w(kBlk), Zm(BB);
+      // M1 = G2^-1/2; the Ritz pairs of M1 H M1 give the rotation M1 Z
+      std::vector<double> M1(BB), Hs(BB), T(BB), C(BB), w(kBlk), Zm(BB);
+      lowdin(G2.data() + i * BB, kBlk, M1.data());
       for (int r = 0; r < kBlk; r++)
         for (int c = 0; c < kBlk; c++)
-          H[r * kBlk + c] = 0.5 * (G[i * BB + r * kBlk + c] + G[i * BB + c * kBlk + r]);
-      gpb::sym_eig(H.data(), kBlk, w.data(), Zm.data());
+          Hs[r * kBlk + c] = 0.5 * (G[i * BB + r * kBlk + c] + G[i * BB + c * kBlk + r]);
+      for (int r = 0; r < kBlk; r++)
+        for (int c = 0; c < kBlk; c++) {
+          double v = 0;
+          for (int k = 0; k < kBlk; k++) v += Hs[r * kBlk + k] * M1[k * kBlk + c];
+          T[r * kBlk + c] = v;
+        }
+      for (int r = 0; r < kBlk; r++)
+        for (int c = 0; c < kBlk; c++) {
+          double v = 0;
+          for (int k = 0; k < kBlk; k++) v += M1[k * kBlk + r] * T[k * kBlk + c];
+          C[r * kBlk + c] = v;
+        }
+      for (int r = 0; r < kBlk; r++)
+        for (int c = r + 1; c < kBlk; c++) C[r * kBlk + c] = C[c * kBlk + r] = 0.5 * (C[r * kBlk + c] + C[c * kBlk + r]);
+      gpb::sym_eig(C.data(), kBlk, w.data(), Zm.data());
       for (int c = 0; c < kBlk; c++) theta[(size_t)i * kBlk + c] = w[c];
-      std::copy(Zm.begin(), Zm.end(), M.begin() + i * BB);
+      for (int r = 0; r < kBlk; r++)
+        for (int c = 0; c < kBlk; c++) {
+          double v = 0;
+          for (int k = 0; k < kBlk; k++) v += M1[r * kBlk + k] * Zm[k * kBlk + c];
+          M[i * BB + r * kBlk + c] = v;
+        }
     });
     CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.btheta, theta.data(), theta.size() * sizeof(double), cudaMemcpyHostToDevice, s));
