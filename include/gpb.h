@@ -123,7 +123,11 @@ typedef enum {
    * (r <= 3, 5, 10, 20, cumulative), cue (L, a, b, texton), counter row
    * (half*16 + slice) and bin -- the raw half-disc histogram counts
    * (sum the two halves of a slice) */
-  GPB_STAGE_COUNTS = 10
+  GPB_STAGE_COUNTS = 10,
+  /* float H*W*9, gpb_warmnet_capture on: the first 9 columns of the
+   * warm-start block (prolongated coarse Ritz vectors), pixel-major, before
+   * the learned correction */
+  GPB_STAGE_WARM0 = 11
 } gpb_stage;
 
 void gpb_default_params(gpb_params* p);
@@ -315,6 +319,23 @@ int32_t gpb_ucm_fit_contours(const uint8_t* bw, uint32_t width, uint32_t height,
 gpb_status gpb_ucm_mean_pb(const double* ws_wt2, const int32_t* labels, uint32_t width, uint32_t height,
                            double* ucm);
 int32_t gpb_ucm_labels_at_scale(const double* ucm2, uint32_t width, uint32_t height, double k, int32_t* labels);
+
+/* ---- Learned correction of the warm start ------------------------------
+ * A two-layer conv net (3 x 3 conv of the start block's first 9 columns and
+ * mPb to 16 channels, ReLU, 1 x 1 conv to 9 corrections) refines the
+ * prolongated coarse Ritz vectors before the fine block solve of
+ * GPB_EIG_WARM.  Weights: W1 [16][10][9], b1 [16], W2 [9][16], b2 [9]
+ * (GPB_WARMNET_PARAMS floats); NULL switches the correction off (the
+ * default).  Training uses gpb_warmnet_grad_device: over n patches given
+ * by their sizes and device arrays of normalised inputs x~ [Ntot][9],
+ * mPb [Ntot] and targets v~ [Ntot][9] (concatenated patch after patch),
+ * the mean squared error and its gradient for the given weights. */
+#define GPB_WARMNET_PARAMS 1609
+gpb_status gpb_warmnet_set(gpb_ctx* ctx, const float* weights, size_t n);
+gpb_status gpb_warmnet_capture(gpb_ctx* ctx, int on);
+gpb_status gpb_warmnet_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                   const float* d_xt, const float* d_mpb, const float* d_vt, const float* weights,
+                                   double* loss, float* grad);
 
 int gpb_device_count(void);
 const char* gpb_status_str(gpb_status s);

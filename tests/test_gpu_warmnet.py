@@ -1,0 +1,59 @@
+"""The learned warm-start correction: the CUDA training kernels against the
+numpy oracle, capture of the start block, and the trained net's effect on
+held-out patches."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import warmnet_oracle as wo  # noqa: E402
+
+GPB_TOL = 1e-3
+
+
+def test_gradient_matches_oracle():
+    """loss and all 1609 partial derivatives of gpb_warmnet_grad_device
+    against the FP64 numpy restatement, on three uneven patches"""
+    torch = pytest.importorskip("torch")
+    import gpb
+    rng = np.random.default_rng(5)
+    pats = []
+    for (H, W) in [(12, 17), (9, 9), (20, 6)]:
+        pats.append((rng.normal(size=(H * W, 9)).astype(np.float32), rng.random(H * W).astype(np.float32),
+                     rng.normal(size=(H * W, 9)).astype(np.float32), H, W))
+    w = wo.init_weights(3, 0.3).astype(np.float32)
+    ctx = gpb.Context()
+    xt = torch.from_numpy(np.concatenate([p[0] for p in pats])).cuda()
+    mp = torch.from_numpy(np.concatenate([p[1] for p in pats])).cuda()
+    vt = torch.from_numpy(np.concatenate([p[2] for p in pats])).cuda()
+    loss, g = ctx.warmnet_grad_device([p[4] for p in pats], [p[3] for p in pats], xt.data_ptr(), mp.data_ptr(),
+                                      vt.data_ptr(), w)
+    ref_l, ref_g = wo.loss_grad(w.astype(np.float64), [(p[0].astype(np.float64), p[1].astype(np.float64),
+                                                        p[2].astype(np.float64), p[3], p[4]) for p in pats])
+    ctx.close()
+    assert abs(loss - ref_l) <= 1e-5 * abs(ref_l)
+    assert np.abs(g - ref_g).max() <= 1e-4 * np.abs(ref_g).max()
+
+
+def test_capture_and_zero_net():
+    """the captured start block comes back per patch; a net of zero weights
+    leaves the result within the parity tolerance of the uncorrected path"""
+    import gpb
+    from gpb import synth
+    img = synth.voronoi_image(96, 112, 40, 6.0, synth.SEED_BASE + 301)
+    cb = synth.make_codebook(img, synth.SEED_BASE + 301, n_sample=1024)
+    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
+    ctx.warmnet_capture(True)
+    ref = ctx.compute_batch([synth.pack_bgr(img)])[0]
+    x0 = ctx.fetch("warm0", 0, (96 * 112, 9), np.float32)
+    assert np.isfinite(x0).all() and np.abs(x0).max() > 0
+    ctx.warmnet_set(np.zeros(gpb.WARMNET_PARAMS, np.float32))
+    got = ctx.compute_batch([synth.pack_bgr(img)])[0]
+    assert ctx.last_status == gpb.GPB_OK
+    assert np.abs(got[0] - ref[0]).max() < GPB_TOL
+    ctx.close()

@@ -26,6 +26,7 @@
 #include "../../include/gpb.h"
 #include "gpb_internal.h"
 #include "k_block.h"
+#include "k_warmnet.h"
 #include "k_eig.h"
 #include "k_static.h"
 #include "kernels.h"
@@ -213,6 +214,13 @@ struct gpb_ctx {
   uint64_t token = 0;          // identifies this context's constant tables
   Buf b;
   std::string last_error;
+  // learned correction of the warm start (k_warmnet.cu): weights, per-patch
+  // scales, and the captured start block of the last batch
+  float* d_wn = nullptr;
+  float* d_wn_scale = nullptr; size_t c_wn_scale = 0;
+  float* d_wn_x0 = nullptr; size_t c_wn_x0 = 0;
+  bool wn_capture = false;
+  int wn_epochs = 0;  // informational, carried with the weights
   // device scratch of the OWT-UCM stage (ucm_api.cpp), freed with the context
   void* ucm_state = nullptr;
   void (*ucm_free)(void*) = nullptr;
@@ -443,6 +451,9 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->ucm_free) ctx->ucm_free(ctx->ucm_state);
+  cudaFree(ctx->d_wn);
+  cudaFree(ctx->d_wn_scale);
+  cudaFree(ctx->d_wn_x0);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   {
     ConstBank& bk = bank_of(ctx->device);
@@ -1228,6 +1239,19 @@ static gpb_status solve_warm(gpb_ctx* ctx, const Layout& L, const Layout& Lc) {
   if (st != GPB_OK) return st;
   CK(cf_launch_prolong(c, (int)L.work16.size(), Xc, b.blk[0], s));
   ctx->launches++;
+  const size_t blk_bytes = (size_t)kBlk * L.lvec * sizeof(float);
+  if (ctx->wn_capture) {  // the start block before any correction, for training
+    CK(grow(ctx->d_wn_x0, ctx->c_wn_x0, (size_t)kBlk * L.lvec));
+    CK(cudaMemcpyAsync(ctx->d_wn_x0, b.blk[0], blk_bytes, cudaMemcpyDeviceToDevice, s));
+  }
+  if (ctx->d_wn) {  // the learned correction of the first 9 columns
+    int max_n = 0;
+    for (const PatchDev& P : L.patches) max_n = std::max(max_n, P.N);
+    CK(grow(ctx->d_wn_scale, ctx->c_wn_scale, np * (size_t)kWnOut));
+    CK(wn_launch_apply(b.patches, (int)np, max_n, b.blk[0], b.mpb, ctx->d_wn, ctx->d_wn_scale, b.blk[1], s));
+    CK(cudaMemcpyAsync(b.blk[0], b.blk[1], blk_bytes, cudaMemcpyDeviceToDevice, s));
+    ctx->launches += 2;
+  }
   Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.afull, 0,
               {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
   float* Xf = nullptr;
@@ -1520,6 +1544,15 @@ extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst
       if (!b.gpbo || !need(8 * N * 4)) return GPB_ERR_ARG;
       e = cudaMemcpy(dst, b.gpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
       break;
+    case GPB_STAGE_WARM0: {  // first 9 columns of the captured start block, pixel-major
+      if (!ctx->d_wn_x0 || !need(N * kWnOut * 4)) return GPB_ERR_ARG;
+      std::vector<float> blk(N * kBlk);
+      e = cudaMemcpy(blk.data(), ctx->d_wn_x0 + (size_t)P.vec * kBlk, N * kBlk * 4, cudaMemcpyDeviceToHost);
+      float* o = (float*)dst;
+      for (size_t i = 0; i < N; i++)
+        for (int c = 0; c < kWnOut; c++) o[i * kWnOut + c] = blk[i * kBlk + c];
+      break;
+    }
     case GPB_STAGE_COUNTS: {
       const size_t per = (size_t)kNannulus * 4 * 32 * 32;
       if (!b.counts || !need(per * N)) return GPB_ERR_ARG;
@@ -1641,3 +1674,64 @@ void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*)) {
   return c->ucm_state;
 }
 }  // namespace gpb
+
+extern "C" gpb_status gpb_warmnet_set(gpb_ctx* ctx, const float* weights, size_t n) {
+  if (!ctx) return GPB_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  if (!weights) {
+    cudaFree(ctx->d_wn);
+    ctx->d_wn = nullptr;
+    return GPB_OK;
+  }
+  if (n != (size_t)kWnParams) return GPB_ERR_ARG;
+  if (!ctx->d_wn) CK(cudaMalloc(&ctx->d_wn, kWnParams * sizeof(float)));
+  CK(cudaMemcpy(ctx->d_wn, weights, kWnParams * sizeof(float), cudaMemcpyHostToDevice));
+  return GPB_OK;
+}
+
+extern "C" gpb_status gpb_warmnet_capture(gpb_ctx* ctx, int on) {
+  if (!ctx) return GPB_ERR_ARG;
+  ctx->wn_capture = on != 0;
+  return GPB_OK;
+}
+
+extern "C" gpb_status gpb_warmnet_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                              const float* d_xt, const float* d_mpb, const float* d_vt,
+                                              const float* weights, double* loss, float* grad) {
+  if (!ctx || n == 0 || !widths || !heights || !d_xt || !d_mpb || !d_vt || !weights || !loss || !grad)
+    return GPB_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->st;
+  std::vector<int4> geo(n);
+  long long tot = 0;
+  int max_n = 0;
+  for (size_t i = 0; i < n; i++) {
+    if (widths[i] == 0 || heights[i] == 0) return GPB_ERR_ARG;
+    geo[i] = make_int4((int)widths[i], (int)heights[i], (int)tot, 0);
+    tot += (long long)widths[i] * heights[i];
+    max_n = std::max(max_n, (int)(widths[i] * heights[i]));
+  }
+  if (tot >= (1ll << 31)) return GPB_ERR_ARG;
+  void* buf = nullptr;
+  const size_t bytes = n * sizeof(int4) + kWnParams * 2 * sizeof(float) + sizeof(double);
+  CK(cudaMalloc(&buf, bytes));
+  int4* d_geo = (int4*)buf;
+  float* d_w = (float*)(d_geo + n);
+  float* d_g = d_w + kWnParams;
+  double* d_l = (double*)(((uintptr_t)(d_g + kWnParams) + 7) & ~(uintptr_t)7);
+  cudaError_t e = cudaMemcpyAsync(d_geo, geo.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, weights, kWnParams * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_g, 0, kWnParams * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_l, 0, sizeof(double), s);
+  if (e == cudaSuccess)
+    e = wn_launch_grad(d_geo, (int)n, max_n, d_xt, d_mpb, d_vt, d_w, 1.0f / (float)(tot * kWnOut), d_g, d_l, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(grad, d_g, kWnParams * sizeof(float), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(loss, d_l, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(buf);
+  if (e != cudaSuccess) {
+    ctx->last_error = cudaGetErrorString(e);
+    return GPB_ERR_CUDA;
+  }
+  return GPB_OK;
+}

@@ -25,7 +25,8 @@ UCM_QUANT, UCM_ARCS, UCM_WSWT, UCM_WSWT2, UCM_REGIONS = range(5)
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
 EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
-          "spb": 7, "cues": 8, "gpb_o": 9, "counts": 10}
+          "spb": 7, "cues": 8, "gpb_o": 9, "counts": 10, "warm0": 11}
+WARMNET_PARAMS = 1609
 
 
 class GpbError(RuntimeError):
@@ -117,6 +118,12 @@ def _lib():
         L.gpb_write_png_minmax.restype = c
         L.gpb_superpixel_features.argtypes = [vp, sz, vp, ctypes.c_int32, c, c, vp]
         L.gpb_superpixel_features.restype = c
+        L.gpb_warmnet_set.argtypes = [vp, vp, sz]
+        L.gpb_warmnet_set.restype = c
+        L.gpb_warmnet_capture.argtypes = [vp, c]
+        L.gpb_warmnet_capture.restype = c
+        L.gpb_warmnet_grad_device.argtypes = [vp, sz, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.gpb_warmnet_grad_device.restype = c
         L.gpb_texton_labels_static.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
         L.gpb_texton_labels_static.restype = c
         u32, i32 = ctypes.c_uint32, ctypes.c_int32
@@ -289,6 +296,31 @@ class Context:
         out = np.empty(shape, dt)
         _check(_lib().gpb_ucm_fetch(self._h, image, what, out.ctypes.data, out.nbytes), "gpb_ucm_fetch")
         return out
+
+    def warmnet_set(self, weights):
+        """Switch the learned warm-start correction on (GPB_WARMNET_PARAMS
+        float weights) or off (None)."""
+        if weights is None:
+            _check(_lib().gpb_warmnet_set(self._h, None, 0), "gpb_warmnet_set")
+            return
+        w = np.ascontiguousarray(weights, np.float32)
+        _check(_lib().gpb_warmnet_set(self._h, w.ctypes.data, w.size), "gpb_warmnet_set")
+
+    def warmnet_capture(self, on=True):
+        _check(_lib().gpb_warmnet_capture(self._h, 1 if on else 0), "gpb_warmnet_capture")
+
+    def warmnet_grad_device(self, widths, heights, d_xt, d_mpb, d_vt, weights):
+        """Mean squared error and gradient of the correction net over patches
+        held on the device (raw pointers); returns (loss, grad)."""
+        w = np.ascontiguousarray(weights, np.float32)
+        ws = np.ascontiguousarray(widths, np.uint32)
+        hs = np.ascontiguousarray(heights, np.uint32)
+        loss = ctypes.c_double()
+        grad = np.empty(WARMNET_PARAMS, np.float32)
+        _check(_lib().gpb_warmnet_grad_device(self._h, len(ws), ws.ctypes.data, hs.ctypes.data, d_xt, d_mpb, d_vt,
+                                              w.ctypes.data, ctypes.byref(loss), grad.ctypes.data),
+               "gpb_warmnet_grad_device")
+        return loss.value, grad
 
     def stats(self):
         s = Stats()
