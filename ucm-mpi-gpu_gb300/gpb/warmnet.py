@@ -38,8 +38,10 @@ def images(n, size, seed):
 
 def collect(ctx, imgs):
     """Runs the warm solve on imgs with the start block captured; returns per
-    image (x~ [N,9], mPb [N], v~ [N,9], H, W): RMS-1 start columns and the
-    converged eigenvectors, RMS 1 and sign-aligned with the start."""
+    image (x~ [N,9], mPb [N], v~ [N,9], H, W): RMS-1 start columns and their
+    projections onto the span of the converged eigenvectors.  The targets
+    depend on that span only, not on how it splits into eigenvectors, so
+    clustered eigenvalues do not make them ambiguous."""
     ctx.warmnet_capture(True)
     ctx.compute_batch([synth.pack_bgr(im) for im in imgs])
     nvec = ctx.params.nvec
@@ -53,17 +55,14 @@ def collect(ctx, imgs):
         nx = np.linalg.norm(x0, axis=0)
         nx[nx == 0] = 1.0
         xt = x0 / nx * np.sqrt(N)
-        nv = np.linalg.norm(v, axis=0)
-        nv[nv == 0] = 1.0
-        vt = v / nv * np.sqrt(N)
-        sign = np.sign((xt * vt).sum(0))
-        sign[sign == 0] = 1.0
-        data.append((xt.astype(np.float32), mpb.astype(np.float32), (vt * sign).astype(np.float32), H, W))
+        q, _ = np.linalg.qr(v)  # orthonormal basis of the eigenvectors' span
+        vt = q @ (q.T @ xt)
+        data.append((xt.astype(np.float32), mpb.astype(np.float32), vt.astype(np.float32), H, W))
     ctx.warmnet_capture(False)
     return data
 
 
-def init_weights(seed=0, scale=0.02):
+def init_weights(seed=0, scale=0.005):
     rng = np.random.default_rng(seed)
     w = np.zeros(NPARAM, np.float32)
     w[:1440] = rng.normal(0.0, scale, 1440)
@@ -126,7 +125,7 @@ def evaluate(cb, imgs, weights):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=0, help="number of 256 x 256 training patches")
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=600)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval", default=None, help="weights to evaluate on held-out 512 x 512 patches")
