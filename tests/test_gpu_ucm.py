@@ -162,3 +162,24 @@ def test_ucm_batch_equals_single_calls(ctx):
     small = ctx.ucm_batch(planes[:2], double_size=False)
     for i in range(2):
         assert np.array_equal(small[i][0], ctx.ucm(planes[i], double_size=False)[0])
+
+
+def test_ucm_rejects_bad_arguments(ctx):
+    """sizes below 2, an empty batch, a NULL plane and an image index past
+    the last call's batch return GPB_ERR_ARG and launch nothing"""
+    import ctypes
+    import gpb
+    L = gpb._lib()
+    out = np.zeros(64, np.float64)
+    planes = np.zeros((8, 4, 4), np.float32)
+    assert L.gpb_ucm(ctx._h, 1, 4, planes.ctypes.data, 0, 1, out.ctypes.data, None) == gpb.GPB_ERR_ARG
+    assert L.gpb_ucm(ctx._h, 4, 4, None, 0, 1, out.ctypes.data, None) == gpb.GPB_ERR_ARG
+    w = np.array([4], np.uint32)
+    ptrs = (ctypes.c_void_p * 1)(planes.ctypes.data)
+    outs = (ctypes.c_void_p * 1)(out.ctypes.data)
+    assert L.gpb_ucm_batch(ctx._h, 0, w.ctypes.data, w.ctypes.data, ptrs, 0, 1, outs, None) == gpb.GPB_ERR_ARG
+    ctx.ucm(_planes(9, 11, 71, 1.0))
+    buf = np.zeros(99, np.uint8)
+    assert L.gpb_ucm_fetch(ctx._h, 1, gpb.UCM_QUANT, buf.ctypes.data, buf.nbytes) == gpb.GPB_ERR_ARG
+    assert L.gpb_ucm_fetch(ctx._h, 0, gpb.UCM_QUANT, buf.ctypes.data, 10) == gpb.GPB_ERR_ARG
+    assert L.gpb_ucm_fetch(ctx._h, 0, gpb.UCM_QUANT, buf.ctypes.data, buf.nbytes) == gpb.GPB_OK
