@@ -45,7 +45,10 @@ namespace ucm {
 // 8-connected components of the non-zero pixels of a row-major H x W map,
 // numbered 1.. in the order of each component's first pixel in row-major
 // order (lib_image.cc:4773-4910 visits elements in linear order and floods
-// each new component).  Union-find with the smaller index as root.
+// each new component).  Two raster passes: provisional labels, in order of
+// their first pixel, with their equivalences in a union-find whose roots
+// are the smallest labels; then each root, taken in label order, is
+// numbered -- which is the order of the components' first pixels.
 static uint32_t find_root(std::vector<uint32_t>& p, uint32_t a) {
   while (p[a] != a) {
     p[a] = p[p[a]];
@@ -56,8 +59,8 @@ static uint32_t find_root(std::vector<uint32_t>& p, uint32_t a) {
 
 uint32_t components8(const uint8_t* bw, int H, int W, std::vector<uint32_t>& lab) {
   const size_t N = (size_t)H * W;
-  std::vector<uint32_t> par(N);
-  for (size_t i = 0; i < N; i++) par[i] = (uint32_t)i;
+  lab.assign(N, 0);
+  std::vector<uint32_t> par(1, 0);  // provisional label 0 is the background
   auto unite = [&](uint32_t a, uint32_t b) {
     a = find_root(par, a);
     b = find_root(par, b);
@@ -65,25 +68,38 @@ uint32_t components8(const uint8_t* bw, int H, int W, std::vector<uint32_t>& lab
     if (a < b) std::swap(a, b);
     par[a] = b;
   };
-  for (int x = 0; x < H; x++)
+  for (int x = 0; x < H; x++) {
+    const uint8_t* r = bw + (size_t)x * W;
+    uint32_t* l = lab.data() + (size_t)x * W;
+    const uint32_t* u = x > 0 ? l - W : nullptr;
     for (int y = 0; y < W; y++) {
-      const uint32_t i = (uint32_t)(x * W + y);
-      if (!bw[i]) continue;
-      if (y > 0 && bw[i - 1]) unite(i, i - 1);
-      if (x > 0) {
-        if (bw[i - W]) unite(i, i - W);
-        if (y > 0 && bw[i - W - 1]) unite(i, i - W - 1);
-        if (y + 1 < W && bw[i - W + 1]) unite(i, i - W + 1);
+      if (!r[y]) continue;
+      uint32_t m = 0;  // the smallest labelled neighbour seen so far
+      auto see = [&](uint32_t v) {
+        if (!v) return;
+        if (!m) m = v;
+        else if (v != m) unite(m, v);
+      };
+      if (y > 0) see(l[y - 1]);
+      if (u) {
+        if (y > 0) see(u[y - 1]);
+        see(u[y]);
+        if (y + 1 < W) see(u[y + 1]);
       }
+      if (!m) {
+        m = (uint32_t)par.size();
+        par.push_back(m);
+      }
+      l[y] = m;
     }
-  lab.assign(N, 0);
-  uint32_t n = 0;
-  for (size_t i = 0; i < N; i++) {
-    if (!bw[i]) continue;
-    const uint32_t r = find_root(par, (uint32_t)i);
-    if (r == i) lab[i] = ++n;  // the root is the component's first pixel
-    else lab[i] = lab[r];
   }
+  std::vector<uint32_t> fin(par.size(), 0);
+  uint32_t n = 0;
+  for (uint32_t v = 1; v < par.size(); v++) {
+    const uint32_t r = find_root(par, v);
+    fin[v] = r == v ? ++n : fin[r];  // a root is its component's first label
+  }
+  for (size_t i = 0; i < N; i++) lab[i] = fin[lab[i]];
   return n;
 }
 
