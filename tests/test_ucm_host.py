@@ -151,3 +151,57 @@ def test_oracle_pins_against_reference(ref, H, W, seed, sigma):
     rl = np.zeros_like(bwl)
     L.ref_ucm_bwlabel(_P(np.ascontiguousarray(bwl)), bwl.shape[0], bwl.shape[1], _P(rl))
     assert np.array_equal(uo.bwlabel(bwl == 1)[0], rl)
+
+
+def _voronoi(H, W, k, rng):
+    ys, xs = rng.integers(0, H, k), rng.integers(0, W, k)
+    yy, xx = np.mgrid[0:H, 0:W]
+    lab, best = np.zeros((H, W), np.int32), np.full((H, W), np.inf)
+    for i in range(k):
+        d = (yy - ys[i]) ** 2 + (xx - xs[i]) ** 2
+        m = d < best
+        best[m], lab[m] = d[m], i
+    return lab
+
+
+def _islands(H, W, step, rng):
+    """square islands of two regions each (left and right half) on a
+    background whose id is the largest: the background's neighbour list is
+    far longer than any island region's, and a half that merges into it
+    still has the other half for a neighbour"""
+    ny, nx = H // step, W // step
+    lab = np.full((H, W), 2 * ny * nx, np.int32)
+    ids = rng.permutation(2 * ny * nx)
+    for i in range(ny):
+        for j in range(nx):
+            s, y0, x0 = int(rng.integers(2, step)), i * step, j * step
+            lab[y0:y0 + s, x0:x0 + s // 2] = ids[2 * (i * nx + j)]
+            lab[y0:y0 + s, x0 + s // 2:x0 + s] = ids[2 * (i * nx + j) + 1]
+    return lab
+
+
+@pytest.mark.parametrize("layout", ["voronoi", "islands"])
+@pytest.mark.parametrize("strength", ["random", "quarters", "flat"])
+def test_merge_layouts_against_reference(ref, layout, strength):
+    """the library's merge on region layouts of many regions (queue entries
+    of merged-away regions dropped in bulk; the father's pairs found through
+    the pair table) and on strengths with many equal energies (ties broken
+    by region ids), against the reference's UcmMeanPb"""
+    import gpb
+    rng = np.random.default_rng(17)
+    H, W = (160, 150) if layout == "voronoi" else (120, 128)
+    lab = _voronoi(H, W, 1500, rng) if layout == "voronoi" else _islands(H, W, 4, rng)
+    G = (2 * H + 1, 2 * W + 1)
+    w2 = {"random": rng.random(G), "quarters": rng.integers(0, 4, G) / 4.0, "flat": np.full(G, 0.5)}[strength]
+    w2 = np.ascontiguousarray(w2)
+    u = np.zeros(G)
+    ref.ref().ref_ucm_mean_pb(_P(w2), _P(lab), H, W, _P(u))
+    assert np.array_equal(gpb.ucm_mean_pb(w2, lab), u)
+
+
+def test_merge_rejects_grids_beyond_32_bit_indices():
+    import gpb
+    L = gpb._lib()
+    one = np.zeros(1)
+    lab = np.zeros(1, np.int32)
+    assert L.gpb_ucm_mean_pb(one.ctypes.data, lab.ctypes.data, 40000, 40000, one.ctypes.data) == gpb.GPB_ERR_ARG

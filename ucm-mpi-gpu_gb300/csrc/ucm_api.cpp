@@ -344,6 +344,8 @@ extern "C" int32_t gpb_ucm_fit_contours(const uint8_t* bw, uint32_t width, uint3
 extern "C" gpb_status gpb_ucm_mean_pb(const double* ws_wt2, const int32_t* labels, uint32_t width, uint32_t height,
                                       double* ucm) {
   if (!ws_wt2 || !labels || !ucm || width == 0 || height == 0) return GPB_ERR_ARG;
+  // grid indices are 32-bit
+  if ((2 * (uint64_t)height + 1) * (2 * (uint64_t)width + 1) >= (1ull << 31)) return GPB_ERR_ARG;
   ucm::mean_pb_merge(ws_wt2, labels, (int)height, (int)width, ucm);
   return GPB_OK;
 }

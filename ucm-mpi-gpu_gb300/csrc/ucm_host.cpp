@@ -18,18 +18,20 @@
 // reference's.
 //
 // The merge restates ComputeUcm (src/ucm_mean_pb.cpp:254-398): the same
-// priority order (energy, region1, region2), the same pushes and the same
-// running sums, so ties break exactly as there.  Boundary elements that
-// became interior are dropped lazily instead of by a scan of the father's
-// list, and the smaller of two element lists is moved into the larger; both
-// leave every update of the map unchanged.
+// priority order (energy, region1, region2), the same running sums in the
+// same order, so ties break exactly as there.  Boundaries are kept as
+// linked lists of segments joined in O(1), pushes that cannot change the
+// pop order are left out, and queue entries of merged-away regions are
+// dropped in bulk; none of this changes a merge or a value of the map.
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
 #include <deque>
 #include <map>
+#include <new>
 #include <queue>
 #include <utility>
 #include <vector>
@@ -677,13 +679,16 @@ int edge_orientation(int x1, int y1, int x2, int y2) {
 namespace {
 
 // One adjacent pair of regions, shared by both sides (the reference keeps a
-// copy in each region's neighbour map; both copies are always updated together).
+// copy in each region's neighbour map; both copies are always updated
+// together).  Its energy is total / length, recomputed where needed.
 struct Pair {
-  double energy = 0, total = 0, length = 0;
+  double total = 0;
   double pushed = -1.0;      // energy and first region of the pair's last queue entry
   double raise = -INFINITY;  // pending raise of the boundary list
+  int32_t length = 0;        // boundary elements
   int first = -1;
-  int head = -1, tail = -1;  // the pair's boundary coordinates: a linked list of nodes
+  int head = -1, tail = -1;  // the pair's boundary: a linked list of segments
+  double energy() const { return total / (double)length; }
 };
 
 // open-addressing map from an unordered region pair to its Pair index
@@ -692,53 +697,168 @@ class PairTable {
   explicit PairTable(size_t expect) {
     size_t c = 16;
     while (c < 2 * expect) c <<= 1;
-    key_.assign(c, kEmpty);
-    val_.assign(c, -1);
+    slot_.assign(c, Slot{kEmpty, -1});
   }
-  // index of pair {a, b}, or -1; with create, a new pair is appended to `pairs`
-  int find(int a, int b, std::vector<Pair>* pairs) {
-    const uint64_t k = a < b ? ((uint64_t)(uint32_t)a << 32) | (uint32_t)b : ((uint64_t)(uint32_t)b << 32) | (uint32_t)a;
-    size_t h = (size_t)((k * 0x9E3779B97F4A7C15ull) >> 20) & (key_.size() - 1);
-    for (;; h = (h + 1) & (key_.size() - 1)) {
-      if (key_[h] == k) return val_[h];
-      if (key_[h] == kEmpty) break;
+  static uint64_t key(int a, int b) {
+    return a < b ? ((uint64_t)(uint32_t)a << 32) | (uint32_t)b : ((uint64_t)(uint32_t)b << 32) | (uint32_t)a;
+  }
+  void insert(uint64_t k, int v) {
+    const size_t mask = slot_.size() - 1;
+    size_t h = hash(k) & mask;
+    while (slot_[h].key != kEmpty) h = (h + 1) & mask;
+    slot_[h] = Slot{k, v};
+    if (++used_ * 2 > slot_.size()) grow();
+  }
+  // index of pair {a, b}; a pair not yet in the map gets index `fresh`
+  // (returned as -fresh - 1, so that the caller can tell)
+  int find_or_add(uint64_t k, int fresh) {
+    const size_t mask = slot_.size() - 1;
+    size_t h = hash(k) & mask;
+    for (;; h = (h + 1) & mask) {
+      if (slot_[h].key == k) return slot_[h].val;
+      if (slot_[h].key == kEmpty) break;
     }
-    if (!pairs) return -1;
-    key_[h] = k;
-    val_[h] = (int)pairs->size();
-    pairs->emplace_back();
-    if (++used_ * 2 > key_.size()) grow();
-    return (int)pairs->size() - 1;
+    slot_[h] = Slot{k, fresh};
+    if (++used_ * 2 > slot_.size()) grow();
+    return -fresh - 1;
   }
 
  private:
+  struct Slot {
+    uint64_t key;
+    int32_t val;
+  };
   static constexpr uint64_t kEmpty = ~0ull;
-  std::vector<uint64_t> key_;
-  std::vector<int> val_;
+  std::vector<Slot> slot_;
   size_t used_ = 0;
+  static size_t hash(uint64_t k) { return (size_t)((k * 0x9E3779B97F4A7C15ull) >> 20); }
   void grow() {
-    std::vector<uint64_t> k2(key_.size() * 2, kEmpty);
-    std::vector<int> v2(key_.size() * 2, -1);
-    for (size_t i = 0; i < key_.size(); i++) {
-      if (key_[i] == kEmpty) continue;
-      size_t h = (size_t)((key_[i] * 0x9E3779B97F4A7C15ull) >> 20) & (k2.size() - 1);
-      while (k2[h] != kEmpty) h = (h + 1) & (k2.size() - 1);
-      k2[h] = key_[i];
-      v2[h] = val_[i];
+    std::vector<Slot> s2(slot_.size() * 2, Slot{kEmpty, -1});
+    const size_t mask = s2.size() - 1;
+    for (const Slot& e : slot_) {
+      if (e.key == kEmpty) continue;
+      size_t h = hash(e.key) & mask;
+      while (s2[h].key != kEmpty) h = (h + 1) & mask;
+      s2[h] = e;
     }
-    key_.swap(k2);
-    val_.swap(v2);
+    slot_.swap(s2);
   }
 };
 
+// A queue entry (energy, region1, region2) in two words: the energy's bits
+// mapped to an unsigned order (negative values reversed, -0 taken as +0),
+// and region1 beside the pair's index.  Region2 is the pair's other region,
+// (region1 ^ (both regions' xor)); it decides only between entries of equal
+// energy and region1.
 struct Entry {
-  double energy;
-  int r1, r2;
-  int pair;  // index of the pair {r1, r2}, fixed while both regions live
-  bool operator>(const Entry& o) const {  // the reference's (energy, region1, region2) order
-    if (energy != o.energy) return energy > o.energy;
-    if (r1 != o.r1) return r1 > o.r1;
-    return r2 > o.r2;
+  uint64_t hi, lo;  // lo: region1 << 32 | pair
+};
+
+inline uint64_t energy_key(double d) {
+  if (d == 0.0) d = 0.0;
+  uint64_t b;
+  memcpy(&b, &d, 8);
+  return (b >> 63) ? ~b : b | (1ull << 63);
+}
+
+inline double key_energy(uint64_t k) {
+  const uint64_t b = (k >> 63) ? k & ~(1ull << 63) : ~k;
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+}
+
+// a 4-ary min-heap of entries in the reference's (energy, region1, region2)
+// order; node i sits at slot i + 3 of a 64-byte aligned buffer, so that the
+// four children of a node share one cache line
+class Queue {
+ public:
+  explicit Queue(const std::vector<int32_t>& pair_xor) : xr_(pair_xor) {}
+  ~Queue() { free(buf_); }
+  Queue(const Queue&) = delete;
+  Queue& operator=(const Queue&) = delete;
+  bool empty() const { return n_ == 0; }
+  size_t size() const { return n_; }
+  void push(const Entry& e) {
+    if (n_ == cap_) grow();
+    size_t i = n_++;
+    while (i > 0) {
+      const size_t par = (i - 1) >> 2;
+      if (!before(e, at(par))) break;
+      at(i) = at(par);
+      i = par;
+    }
+    at(i) = e;
+  }
+  // entries appended unordered, then ordered at once (bottom-up)
+  void append(const Entry& e) {
+    if (n_ == cap_) grow();
+    at(n_++) = e;
+  }
+  void heapify() {
+    if (n_ < 2) return;
+    for (size_t i = (n_ - 2) >> 2;; i--) {
+      down(i, at(i));
+      if (i == 0) break;
+    }
+  }
+  // drops the entries that keep() rejects, then reorders the rest
+  template <class Keep>
+  void filter(Keep keep) {
+    size_t w = 0;
+    for (size_t i = 0; i < n_; i++) {
+      const Entry e = at(i);
+      if (keep(e)) at(w++) = e;
+    }
+    n_ = w;
+    heapify();
+  }
+  Entry pop() {
+    const Entry top = at(0);
+    n_--;
+    if (n_ > 0) down(0, at(n_));
+    return top;
+  }
+
+ private:
+  const std::vector<int32_t>& xr_;
+  Entry* buf_ = nullptr;
+  size_t n_ = 0, cap_ = 0;
+  Entry& at(size_t i) { return buf_[i + 3]; }
+  bool before(const Entry& a, const Entry& b) const {
+    if (a.hi != b.hi) return a.hi < b.hi;
+    const uint32_t r1a = (uint32_t)(a.lo >> 32), r1b = (uint32_t)(b.lo >> 32);
+    if (r1a != r1b) return r1a < r1b;
+    return ((uint32_t)xr_[(uint32_t)a.lo] ^ r1a) < ((uint32_t)xr_[(uint32_t)b.lo] ^ r1b);
+  }
+  void grow() {
+    const size_t cap = cap_ ? 2 * cap_ : 1024;
+    Entry* nb = (Entry*)aligned_alloc(64, ((cap + 4) * sizeof(Entry) + 63) / 64 * 64);
+    if (!nb) throw std::bad_alloc();
+    if (buf_) memcpy(nb + 3, buf_ + 3, n_ * sizeof(Entry));
+    free(buf_);
+    buf_ = nb;
+    cap_ = cap;
+  }
+  // place e at the hole i, moving smaller children up
+  void down(size_t i, const Entry e) {
+    for (;;) {
+      const size_t c0 = 4 * i + 1;
+      if (c0 >= n_) break;
+      size_t best = c0;
+      if (c0 + 3 < n_) {
+        const size_t b01 = before(at(c0 + 1), at(c0)) ? c0 + 1 : c0;
+        const size_t b23 = before(at(c0 + 3), at(c0 + 2)) ? c0 + 3 : c0 + 2;
+        best = before(at(b23), at(b01)) ? b23 : b01;
+      } else {
+        for (size_t c = c0 + 1; c < n_; c++)
+          if (before(at(c), at(best))) best = c;
+      }
+      if (!before(at(best), e)) break;
+      at(i) = at(best);
+      i = best;
+    }
+    at(i) = e;
   }
 };
 
@@ -749,17 +869,25 @@ struct Entry {
 // column-major; the grid coordinates are the same).  lb: local boundary
 // strengths; part: H x W region ids 0..n-1 (negative ids are skipped).
 //
-// The reference sums each pair's boundary strengths in column-major order
-// of the coordinates; the grid is walked in that order here.
+// The boundary elements (grid points between two 4-adjacent pixels of
+// different regions) are numbered in the reference's column-major order:
+// grid column 2y holds the (odd, even) points between horizontal
+// neighbours (x, y-1), (x, y); grid column 2y+1 the (even, odd) ones
+// between vertical neighbours (x-1, y), (x, y).  A stable two-pass
+// counting sort by (smaller id, larger id) groups them by pair, each
+// pair's elements still in that order, so every pair's sum of strengths
+// runs in the reference's order.  The elements of one initial pair form a
+// segment.
 //
 // The reference walks the son's whole boundary on every merge, raising the
 // map to the merge's saliency.  Here each pair of regions keeps one linked
-// list of its boundary coordinates: the son-father list takes the saliency
-// when it closes, the son's other lists are joined to the father's in O(1).
-// With saliencies that never decrease -- the reference stops
-// being defined otherwise: it frees its arrays and carries on -- every
-// coordinate ends at the saliency of the merge that joins its two sides,
-// as there.
+// list of segments: the son-father list takes the saliency when it
+// closes, the son's other lists are joined to the father's in O(1).  With
+// saliencies that never decrease -- the reference stops being defined
+// otherwise: it frees its arrays and carries on -- every element ends at
+// the saliency of the merge that joins its two sides, as there.  Each
+// segment is closed exactly once, so its value is recorded per segment and
+// written to the map at the end, in element order.
 //
 // After every merge the reference pushes (d, k, father) for each neighbour
 // k of the father.  A push identical to the pair's last entry still in the
@@ -772,135 +900,226 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
   const int GW = 2 * W + 1, GH = 2 * H + 1;
   int n = 0;
   for (size_t p = 0; p < (size_t)H * W; p++) n = std::max(n, part[p] + 1);
-  for (size_t i = 0; i < (size_t)GH * GW; i++) ucm[i] = 0.0;
-  if (n <= 0) return;
+  if (n <= 0) {
+    memset(ucm, 0, sizeof(double) * (size_t)GH * GW);
+    return;
+  }
+  // boundary elements in row-major grid order: regions (a < b), grid index,
+  // grid column and strength
+  std::vector<int32_t> ea, eb, ec, ecol;
+  std::vector<double> ev;
+  {
+    size_t cnt = 0;
+    for (int x = 0; x < H; x++) {
+      const int32_t* row = part + (size_t)x * W;
+      if (x > 0)
+        for (int y = 0; y < W; y++) cnt += row[y - W] != row[y];
+      for (int y = 1; y < W; y++) cnt += row[y - 1] != row[y];
+    }
+    ea.reserve(cnt);
+    eb.reserve(cnt);
+    ec.reserve(cnt);
+    ecol.reserve(cnt);
+    ev.reserve(cnt);
+  }
+  auto emit = [&](int a, int b, int32_t coord, int32_t col) {
+    if (a < 0 || b < 0) return;
+    ea.push_back(std::min(a, b));
+    eb.push_back(std::max(a, b));
+    ec.push_back(coord);
+    ecol.push_back(col);
+    ev.push_back((double)lb[coord]);
+  };
+  for (int x = 0; x < H; x++) {
+    const int32_t* row = part + (size_t)x * W;
+    if (x > 0) {  // grid row 2x: (even, odd) points between pixel rows x-1 and x
+      const int32_t* above = row - W;
+      const int32_t base = 2 * x * GW + 1;
+      for (int y = 0; y < W; y++)
+        if (above[y] != row[y]) emit(above[y], row[y], base + 2 * y, 2 * y + 1);
+    }
+    const int32_t base = (2 * x + 1) * GW;  // grid row 2x+1: (odd, even) points within pixel row x
+    for (int y = 1; y < W; y++)
+      if (row[y - 1] != row[y]) emit(row[y - 1], row[y], base + 2 * y, 2 * y);
+  }
+  const int32_t ne = (int32_t)ea.size();
+  // stable counting sorts by grid column, then b, then a: order[i] is the
+  // i-th element in (a, b, column-major) order
+  std::vector<int32_t> order(ne), seg(ne), cnt((size_t)std::max(n, GW) + 1);
+  auto count_sort = [&](const std::vector<int32_t>& key, int nkey, const int32_t* in, int32_t* out) {
+    std::fill(cnt.begin(), cnt.begin() + nkey + 1, 0);
+    for (int32_t i = 0; i < ne; i++) cnt[key[i] + 1]++;
+    for (int c = 0; c < nkey; c++) cnt[c + 1] += cnt[c];
+    for (int32_t i = 0; i < ne; i++) {
+      const int32_t e = in ? in[i] : i;
+      out[cnt[key[e]]++] = e;
+    }
+  };
+  count_sort(ecol, GW, nullptr, order.data());
+  std::vector<int32_t>().swap(ecol);
+  count_sort(eb, n, order.data(), seg.data());
+  // the last pass, by a, carries each element's regions and strength along
+  std::vector<int32_t> sa(ne), sb(ne);
+  std::vector<double> sv(ne);
+  std::fill(cnt.begin(), cnt.begin() + n + 1, 0);
+  for (int32_t i = 0; i < ne; i++) cnt[ea[i] + 1]++;
+  for (int c = 0; c < n; c++) cnt[c + 1] += cnt[c];
+  for (int32_t i = 0; i < ne; i++) {
+    const int32_t e = seg[i], q = cnt[ea[e]]++;
+    order[q] = e;
+    sa[q] = ea[e];
+    sb[q] = eb[e];
+    sv[q] = ev[e];
+  }
+  std::vector<int32_t>().swap(eb);
+  std::vector<int32_t>().swap(ea);
+  std::vector<double>().swap(ev);
+  // the initial pairs in (a, b) order, one segment each; seg[e] is element
+  // e's segment
+  std::vector<Pair> P;
+  std::vector<int32_t> pa, pxor;  // each pair's a, and a ^ b
+  for (int32_t i = 0; i < ne;) {
+    const int32_t a = sa[i], b = sb[i];
+    const int32_t p = (int32_t)P.size();
+    double total = 0.0;
+    int32_t j = i;
+    for (; j < ne && sa[j] == a && sb[j] == b; j++) {
+      total += sv[j];
+      seg[order[j]] = p;
+    }
+    Pair pr;
+    pr.total = total;
+    pr.length = j - i;
+    pr.head = pr.tail = p;
+    P.push_back(pr);
+    pa.push_back(a);
+    pxor.push_back(a ^ b);
+    i = j;
+  }
+  std::vector<int32_t>().swap(order);
+  std::vector<int32_t>().swap(sa);
+  std::vector<int32_t>().swap(sb);
+  std::vector<double>().swap(sv);
+  const int np0 = (int)P.size();
+  P.reserve(3 * (size_t)np0);
+  pxor.reserve(3 * (size_t)np0);
+  std::vector<int32_t> snext(np0, -1);  // segment lists
+  std::vector<double> sval(np0);        // each segment's value when its list closes
+  // neighbour lists (neighbour, pair index)
+  std::vector<std::vector<std::pair<int, int>>> nb(n);
+  {
+    std::vector<int32_t> deg(n, 0);
+    for (int p = 0; p < np0; p++) {
+      deg[pa[p]]++;
+      deg[pa[p] ^ pxor[p]]++;
+    }
+    for (int c = 0; c < n; c++) nb[c].reserve(deg[c] + 8);
+  }
+  // each region's pairs whose last entry has it first, as linked lists of
+  // (pushing region, pair)
+  struct Pend {
+    int32_t b, pair, next;
+  };
+  std::vector<Pend> pend;
+  pend.reserve((size_t)np0 * 3);
+  std::vector<int32_t> phead(n, -1);
   std::vector<int> up(n);  // union-find; a root is a live region, its id the father's
   for (int c = 0; c < n; c++) up[c] = c;
-  std::vector<Pair> P;
-  P.reserve((size_t)n * 8);
-  PairTable T((size_t)n * 8);
-  // each pair's boundary coordinates as a linked list of nodes (coordinate,
-  // next); lists are joined in O(1) when their pairs join
-  std::vector<int32_t> node_coord, node_next;
-  node_coord.reserve((size_t)H * W);
-  node_next.reserve((size_t)H * W);
-  std::vector<std::vector<std::pair<int, int>>> nb(n), pending(n);  // (neighbour, pair index)
-  // Boundary coordinates in the reference's column-major order, so that
-  // each pair's sum runs in that order: grid column 2y holds the (odd, even)
-  // coordinates between horizontal neighbours (x, y-1), (x, y); grid column
-  // 2y+1 the (even, odd) ones between vertical neighbours (x-1, y), (x, y).
-  // A transposed copy of the labels makes the walk sequential.
-  std::vector<int32_t> tr((size_t)H * W);
-  for (int x0 = 0; x0 < H; x0 += 32)
-    for (int y0 = 0; y0 < W; y0 += 32)
-      for (int x = x0; x < std::min(H, x0 + 32); x++)
-        for (int y = y0; y < std::min(W, y0 + 32); y++) tr[(size_t)y * H + x] = part[(size_t)x * W + y];
-  int last_a = -1, last_b = -1, last_p = -1;  // runs repeat a pair
-  auto add = [&](int a, int b, int32_t coord) {
-    if (a < 0 || b < 0 || a == b) return;
-    int pi;
-    if (a == last_a && b == last_b) {
-      pi = last_p;
-    } else {
-      const size_t np = P.size();
-      pi = T.find(a, b, &P);
-      if (P.size() != np) {
-        nb[a].push_back({b, pi});
-        nb[b].push_back({a, pi});
-      }
-      last_a = a;
-      last_b = b;
-      last_p = pi;
-    }
-    Pair& pr = P[pi];
-    const int32_t nd = (int32_t)node_coord.size();
-    node_coord.push_back(coord);
-    node_next.push_back(-1);
-    if (pr.tail < 0) pr.head = nd;
-    else node_next[pr.tail] = nd;
-    pr.tail = nd;
-    pr.total += (double)lb[coord];
-    pr.length += 1.0;
-  };
-  for (int y = 0; y < W; y++) {
-    const int32_t* cur = tr.data() + (size_t)y * H;
-    if (y > 0) {
-      const int32_t* left = cur - H;
-      for (int x = 0; x < H; x++) add(left[x], cur[x], (2 * x + 1) * GW + 2 * y);
-    }
-    for (int x = 1; x < H; x++) add(cur[x - 1], cur[x], (2 * x) * GW + 2 * y + 1);
+  // entries of merged-away regions never pass the label check; they are
+  // dropped from the queue in bulk once they make up about half of it.
+  // qcnt: queue entries naming each region; dead: sum over entries of their
+  // merged-away regions (between 1x and 2x the dead entries)
+  std::vector<int32_t> qcnt(n, 0);
+  size_t dead = 0;
+  Queue Q(pxor);
+  for (int p = 0; p < np0; p++) {
+    const int a = pa[p], b = pa[p] ^ pxor[p];
+    nb[a].push_back({b, p});
+    nb[b].push_back({a, p});
+    Pair& pr = P[p];
+    const double d = pr.energy();
+    Q.append({energy_key(d), ((uint64_t)(uint32_t)a << 32) | (uint32_t)p});
+    qcnt[a]++;
+    qcnt[b]++;
+    pr.pushed = d;
+    pr.first = a;
+    pend.push_back({b, p, phead[a]});
+    phead[a] = (int32_t)pend.size() - 1;
   }
-  std::vector<int32_t>().swap(tr);
-  // a 4-ary min-heap in the reference's (energy, region1, region2) order
-  std::vector<Entry> heap;
-  heap.reserve(P.size() * 2);
-  auto before = [](const Entry& a, const Entry& b) { return b > a; };
-  auto heap_push = [&](const Entry& e) {
-    size_t i = heap.size();
-    heap.push_back(e);
-    while (i > 0) {
-      const size_t par = (i - 1) / 4;
-      if (!before(heap[i], heap[par])) break;
-      std::swap(heap[i], heap[par]);
-      i = par;
-    }
-  };
-  auto heap_pop = [&]() {
-    const Entry top = heap[0];
-    heap[0] = heap.back();
-    heap.pop_back();
-    const size_t sz = heap.size();
-    size_t i = 0;
-    for (;;) {
-      const size_t c0 = 4 * i + 1;
-      if (c0 >= sz) break;
-      size_t best = c0;
-      const size_t ce = std::min(c0 + 4, sz);
-      for (size_t c = c0 + 1; c < ce; c++)
-        if (before(heap[c], heap[best])) best = c;
-      if (!before(heap[best], heap[i])) break;
-      std::swap(heap[i], heap[best]);
-      i = best;
-    }
-    return top;
-  };
+  std::vector<int32_t>().swap(pa);
+  Q.heapify();
   auto push = [&](int pi, double d, int a, int b) {  // entry (d, a, b); b is the region that pushes
-    heap_push({d, a, b, pi});
+    Q.push({energy_key(d), ((uint64_t)(uint32_t)a << 32) | (uint32_t)pi});
+    qcnt[a]++;
+    qcnt[b]++;
     P[pi].pushed = d;
     P[pi].first = a;
-    pending[a].push_back({b, pi});
+    pend.push_back({b, pi, phead[a]});
+    phead[a] = (int32_t)pend.size() - 1;
   };
-  for (int c = 0; c < n; c++)
-    for (const auto& kp : nb[c])
-      if (kp.first > c) {
-        Pair& pr = P[kp.second];
-        pr.energy = pr.total / pr.length;
-        push(kp.second, pr.energy, c, kp.first);
-      }
-  auto flush = [&](Pair& pr, double extra) {
+  auto close = [&](Pair& pr, double extra) {
     const double r = std::max(pr.raise, extra);
-    for (int32_t k = pr.head; k >= 0; k = node_next[k])
-      if (ucm[node_coord[k]] < r) ucm[node_coord[k]] = r;
+    for (int32_t s = pr.head; s >= 0; s = snext[s]) sval[s] = r;
     pr.head = pr.tail = -1;
   };
   std::vector<std::pair<int, int>> touched;
-  while (!heap.empty()) {
-    const Entry m = heap_pop();
-    if (up[m.r1] != m.r1 || up[m.r2] != m.r2) continue;
-    const int ci = m.pair;  // both regions live, so the pair is the one pushed
-    if (m.energy != P[ci].energy) continue;
-    const double saliency = P[ci].total / P[ci].length;
-    const int son = std::min(m.r1, m.r2), father = std::max(m.r1, m.r2);
-    flush(P[ci], saliency);  // the son-father boundary becomes interior
+  // the father's pairs by neighbour, for the current merge (mark == merge count)
+  std::vector<int32_t> fpair(n), mark(n, -1), nlive(n, 0);
+  int32_t merges = 0;
+  // the pairs of live regions by key, built when first needed
+  PairTable T(0);
+  bool table = false;
+  while (!Q.empty()) {
+    const Entry m = Q.pop();
+    const int r1 = (int)(m.lo >> 32), pi = (int)(uint32_t)m.lo;
+    const int r2 = r1 ^ pxor[pi];
+    qcnt[r1]--;
+    qcnt[r2]--;
+    if (up[r1] != r1 || up[r2] != r2) {
+      dead -= (up[r1] != r1) + (up[r2] != r2);
+      continue;
+    }
+    const double saliency = P[pi].energy();  // both regions live, so the pair is current
+    if (key_energy(m.hi) != saliency) continue;
+    const int son = std::min(r1, r2), father = std::max(r1, r2);
+    close(P[pi], saliency);  // the son-father boundary becomes interior
     up[son] = father;
-    // the son's live neighbours other than the father join the father's
+    dead += qcnt[son];
+    // the son's live neighbours other than the father join the father's;
+    // the father's pairs come from its list, or, where that list is much
+    // longer than the son's, from the table
     touched.clear();
+    const bool by_list = nb[father].size() <= 16 * nb[son].size() + 64;
+    if (by_list)
+      for (const auto& kp : nb[father]) {
+        fpair[kp.first] = kp.second;
+        mark[kp.first] = merges;
+      }
     for (const auto& kp : nb[son]) {
       const int k = kp.first, si = kp.second;
       if (up[k] != k || k == father) continue;
-      const size_t np = P.size();
-      const int fi = T.find(father, k, &P);
-      if (P.size() != np) {
+      int fi;
+      if (by_list) {  // a live neighbour missing from the father's list has no pair yet
+        if (mark[k] == merges) {
+          fi = fpair[k];
+        } else {
+          fi = -(int)P.size() - 1;
+          if (table) T.insert(PairTable::key(father, k), (int)P.size());
+        }
+      } else {
+        if (!table) {
+          for (int c = 0; c < n; c++)
+            if (up[c] == c)
+              for (const auto& kq : nb[c])
+                if (kq.first > c && up[kq.first] == kq.first) T.insert(PairTable::key(c, kq.first), kq.second);
+          table = true;
+        }
+        fi = T.find_or_add(PairTable::key(father, k), (int)P.size());
+      }
+      if (fi < 0) {
+        fi = -fi - 1;
+        P.emplace_back();
+        pxor.push_back(father ^ k);
         nb[father].push_back({k, fi});
         nb[k].push_back({father, fi});
       }
@@ -912,46 +1131,76 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
       // they are and keep the larger pending raise
       if (s.head >= 0) {
         if (f.head < 0) f.head = s.head;
-        else node_next[f.tail] = s.head;
+        else snext[f.tail] = s.head;
         f.tail = s.tail;
         f.raise = std::max(f.raise, std::max(s.raise, saliency));
         s.head = s.tail = -1;
       }
       touched.push_back({k, fi});
     }
+    merges++;
     std::vector<std::pair<int, int>>().swap(nb[son]);
-    std::vector<std::pair<int, int>>().swap(pending[son]);
-    for (const auto& kp : pending[father]) touched.push_back(kp);
-    std::vector<std::pair<int, int>>().swap(pending[father]);
+    phead[son] = -1;
+    for (int32_t q = phead[father]; q >= 0; q = pend[q].next) touched.push_back({pend[q].b, pend[q].pair});
+    phead[father] = -1;
     for (const auto& kp : touched) {
       const int k = kp.first;
       if (up[k] != k || k == father) continue;
-      Pair& f = P[kp.second];
-      const double d = f.total / f.length;
-      f.energy = d;
+      const Pair& f = P[kp.second];
+      const double d = f.energy();
       if (!(f.pushed == d && f.first == k)) push(kp.second, d, k, father);
     }
-    if (nb[father].size() > 64) {  // drop merged-away neighbours now and then
+    if (dead >= Q.size() && Q.size() >= 1024) {
+      Q.filter([&](const Entry& e) {
+        const int a = (int)(e.lo >> 32), b = a ^ pxor[(uint32_t)e.lo];
+        if (up[a] == a && up[b] == b) return true;
+        qcnt[a]--;
+        qcnt[b]--;
+        return false;
+      });
+      dead = 0;
+    }
+    // drop merged-away neighbours from the father's list once it has grown
+    // to twice its live length at the last drop (amortised O(1) a merge)
+    if (nb[father].size() >= 2 * (size_t)nlive[father] + 64) {
       std::vector<std::pair<int, int>>& v = nb[father];
       size_t w = 0;
       for (size_t r = 0; r < v.size(); r++)
         if (up[v[r].first] == v[r].first) v[w++] = v[r];
       v.resize(w);
+      nlive[father] = (int32_t)w;
     }
   }
   for (Pair& pr : P)  // boundaries never closed (a split adjacency graph)
-    if (pr.head >= 0) flush(pr, -INFINITY);
-  // CompleteContourMap: every even-even grid point takes the largest of its
-  // four neighbours (starting from 0)
-  for (int x = 0; x < GH; x += 2)
+    if (pr.head >= 0) close(pr, -INFINITY);
+  // the map row by row: zeros, then each element raised once to its
+  // segment's value; then CompleteContourMap on the even rows: every
+  // even-even point takes the largest of its four neighbours (from 0)
+  int32_t e = 0;
+  auto fill_row = [&](int r) {
+    double* out = ucm + (size_t)r * GW;
+    memset(out, 0, sizeof(double) * GW);
+    const int32_t end = (r + 1) * GW;
+    for (; e < ne && ec[e] < end; e++) {
+      const double v = sval[seg[e]];
+      if (v > 0.0) ucm[ec[e]] = v;
+    }
+  };
+  for (int x = 0; x < GH; x += 2) {
+    fill_row(x);
+    if (x + 1 < GH) fill_row(x + 1);
+    double* row = ucm + (size_t)x * GW;
+    const double* below = x + 1 < GH ? row + GW : nullptr;
+    const double* above = x >= 1 ? row - GW : nullptr;
     for (int y = 0; y < GW; y += 2) {
       double m = 0.0;
-      if (x + 1 < GH && m < ucm[(size_t)(x + 1) * GW + y]) m = ucm[(size_t)(x + 1) * GW + y];
-      if (y + 1 < GW && m < ucm[(size_t)x * GW + y + 1]) m = ucm[(size_t)x * GW + y + 1];
-      if (x >= 1 && m < ucm[(size_t)(x - 1) * GW + y]) m = ucm[(size_t)(x - 1) * GW + y];
-      if (y >= 1 && m < ucm[(size_t)x * GW + y - 1]) m = ucm[(size_t)x * GW + y - 1];
-      ucm[(size_t)x * GW + y] = m;
+      if (below && m < below[y]) m = below[y];
+      if (y + 1 < GW && m < row[y + 1]) m = row[y + 1];
+      if (above && m < above[y]) m = above[y];
+      if (y >= 1 && m < row[y - 1]) m = row[y - 1];
+      row[y] = m;
     }
+  }
 }
 
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm) {
