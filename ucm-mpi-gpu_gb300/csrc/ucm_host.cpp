@@ -164,11 +164,12 @@ class Contours {
   std::vector<Edge> edge;
 
  private:
-  std::vector<uint32_t> lab_;
+  const uint8_t* bw_ = nullptr;  // the arcs (non-zero); 8-neighbours of an arc pixel that are
+                                 // arcs are in its component
   std::vector<uint8_t> is_v_, is_e_;
   std::vector<int32_t> assign_;
 
-  uint32_t lab(int x, int y) const { return lab_[(size_t)x * W_ + y]; }
+  bool arc(int x, int y) const { return bw_[(size_t)x * W_ + y] != 0; }
   void build(const uint8_t* bw);
   void trace(int v_id, int x, int y);
   int add_vertex(int x, int y) {
@@ -216,47 +217,94 @@ size_t Contours::farthest(const Edge& e) const {
 
 void Contours::build(const uint8_t* bw) {
   const size_t N = (size_t)H_ * W_;
-  const uint32_t nl = components8(bw, H_, W_, lab_);
+  bw_ = bw;
   is_v_.assign(N, 0);
   is_e_.assign(N, 0);
   assign_.assign(N, 0);
-  std::vector<uint8_t> has_v(nl, 0);
-  std::vector<int> last_x(nl, 0), last_y(nl, 0);
-  for (int x = 0; x < H_; x++)
+  // One raster pass: the pattern vertices in row-major order, and the
+  // 8-connected components as provisional labels (two rows at a time) whose
+  // equivalences go to a union-find with the smallest label as root, as in
+  // components8; per provisional label whether it holds a vertex and its
+  // last pixel.
+  std::vector<uint32_t> par(1, 0), rows(2 * (size_t)W_, 0);
+  std::vector<uint8_t> pv(1, 0);
+  std::vector<size_t> plast(1, 0);
+  auto unite = [&](uint32_t a, uint32_t b) {
+    a = find_root(par, a);
+    b = find_root(par, b);
+    if (a == b) return;
+    if (a < b) std::swap(a, b);
+    par[a] = b;
+  };
+  for (int x = 0; x < H_; x++) {
+    const uint8_t* r = bw + (size_t)x * W_;
+    const uint8_t* rn = x + 1 < H_ ? r + W_ : nullptr;  // the reference's e side
+    const uint8_t* rp = x > 0 ? r - W_ : nullptr;       // w side
+    uint32_t* l = rows.data() + (size_t)(x & 1) * W_;
+    const uint32_t* u = x > 0 ? rows.data() + (size_t)((x + 1) & 1) * W_ : nullptr;
     for (int y = 0; y < W_; y++) {
-      const uint32_t l = lab(x, y);
-      if (!l) continue;
-      unsigned m = 0;
-      const bool hn = y + 1 < W_, hs = y > 0, he = x + 1 < H_, hw = x > 0;
-      if (hn && lab(x, y + 1) == l) m |= BN;
-      if (hs && lab(x, y - 1) == l) m |= BS;
-      if (he && lab(x + 1, y) == l) m |= BE;
-      if (hw && lab(x - 1, y) == l) m |= BW;
-      if (hn && he && lab(x + 1, y + 1) == l) m |= BNE;
-      if (hn && hw && lab(x - 1, y + 1) == l) m |= BNW;
-      if (hs && he && lab(x + 1, y - 1) == l) m |= BSE;
-      if (hs && hw && lab(x - 1, y - 1) == l) m |= BSW;
-      if (kVertex.v[m]) {
-        add_vertex(x, y);
-        has_v[l - 1] = 1;
+      if (!r[y]) {
+        l[y] = 0;
+        continue;
       }
-      last_x[l - 1] = x;
-      last_y[l - 1] = y;
+      uint32_t m = 0;  // the smallest labelled neighbour seen so far
+      auto see = [&](uint32_t v) {
+        if (!v) return;
+        if (!m) m = v;
+        else if (v != m) unite(m, v);
+      };
+      if (y > 0) see(l[y - 1]);
+      if (u) {
+        if (y > 0) see(u[y - 1]);
+        see(u[y]);
+        if (y + 1 < W_) see(u[y + 1]);
+      }
+      if (!m) {
+        m = (uint32_t)par.size();
+        par.push_back(m);
+        pv.push_back(0);
+        plast.push_back(0);
+      }
+      l[y] = m;
+      const bool hn = y + 1 < W_, hs = y > 0;
+      unsigned k = 0;
+      if (hn && r[y + 1]) k |= BN;
+      if (hs && r[y - 1]) k |= BS;
+      if (rn && rn[y]) k |= BE;
+      if (rp && rp[y]) k |= BW;
+      if (hn && rn && rn[y + 1]) k |= BNE;
+      if (hn && rp && rp[y + 1]) k |= BNW;
+      if (hs && rn && rn[y - 1]) k |= BSE;
+      if (hs && rp && rp[y - 1]) k |= BSW;
+      if (kVertex.v[k]) {
+        add_vertex(x, y);
+        pv[m] = 1;
+      }
+      plast[m] = (size_t)x * W_ + y;
     }
-  for (uint32_t l = 0; l < nl; l++)  // a closed loop: its last pixel becomes a vertex
-    if (!has_v[l]) add_vertex(last_x[l], last_y[l]);
+  }
+  // each component (a root, in the order of the components' first pixels)
+  // without a vertex is a closed loop: its last pixel becomes a vertex
+  std::vector<uint8_t> rv(par.size(), 0);
+  std::vector<size_t> rlast(par.size(), 0);
+  for (uint32_t v = 1; v < par.size(); v++) {
+    const uint32_t r = find_root(par, v);
+    rv[r] |= pv[v];
+    rlast[r] = std::max(rlast[r], plast[v]);
+  }
+  for (uint32_t v = 1; v < par.size(); v++)
+    if (par[v] == v && !rv[v]) add_vertex((int)(rlast[v] / W_), (int)(rlast[v] % W_));
   for (size_t v_id = 0; v_id < vert.size(); v_id++) {  // grows while tracing
     const int vx = vert[v_id].x, vy = vert[v_id].y;
-    const uint32_t l = lab(vx, vy);
     int qx[8], qy[8], nq = 0;
     const int x0 = vx > 0 ? vx - 1 : vx + 1, y0 = vy > 0 ? vy - 1 : vy + 1;
     for (int x = x0; x <= vx + 1 && x < H_; x += 2)
-      if (lab(x, vy) == l) qx[nq] = x, qy[nq++] = vy;
+      if (arc(x, vy)) qx[nq] = x, qy[nq++] = vy;
     for (int y = y0; y <= vy + 1 && y < W_; y += 2)
-      if (lab(vx, y) == l) qx[nq] = vx, qy[nq++] = y;
+      if (arc(vx, y)) qx[nq] = vx, qy[nq++] = y;
     for (int x = x0; x <= vx + 1 && x < H_; x += 2)
       for (int y = y0; y <= vy + 1 && y < W_; y += 2)
-        if (lab(x, y) == l && lab(vx, y) != l && lab(x, vy) != l) qx[nq] = x, qy[nq++] = y;
+        if (arc(x, y) && !arc(vx, y) && !arc(x, vy)) qx[nq] = x, qy[nq++] = y;
     for (int k = 0; k < nq; k++) {
       const size_t i = (size_t)qx[k] * W_ + qy[k];
       if (is_v_[i]) {
@@ -289,7 +337,6 @@ void Contours::build(const uint8_t* bw) {
 // vertices, until a vertex or a dead end (which becomes a new vertex).
 void Contours::trace(int v_id, int x, int y) {
   const size_t iv = (size_t)vert[v_id].x * W_ + vert[v_id].y;
-  const uint32_t l = lab_[iv];
   const int e_id = (int)edge.size();
   std::vector<int32_t> px;
   is_e_[iv] = 1;
@@ -300,22 +347,29 @@ void Contours::trace(int v_id, int x, int y) {
     is_e_[i] = 1;
     assign_[i] = e_id;
     const bool hn = y + 1 < W_, hs = y > 0, he = x + 1 < H_, hw = x > 0;
-    auto av = [&](bool has, size_t j) { return has && lab_[j] == l && !is_e_[j]; };
+    auto av = [&](bool has, size_t j) { return has && bw_[j] && !is_e_[j]; };
     const size_t in = i + 1, is = i - 1, ie = i + W_, iw = i - W_;
-    const bool an = av(hn, in), as = av(hs, is), ae = av(he, ie), aw = av(hw, iw);
-    const bool ane = av(hn && he, ie + 1), anw = av(hn && hw, iw + 1), ase = av(hs && he, ie - 1),
-               asw = av(hs && hw, iw - 1);
+    // each neighbour's state is read when its rule comes up (nothing
+    // changes between the rules)
+    const bool an = av(hn, in);
     if (an && !is_v_[in]) { y++; continue; }
+    const bool as = av(hs, is);
     if (as && !is_v_[is]) { y--; continue; }
+    const bool ae = av(he, ie);
     if (ae && !is_v_[ie]) { x++; continue; }
+    const bool aw = av(hw, iw);
     if (aw && !is_v_[iw]) { x--; continue; }
     if (an) { y++; break; }
     if (as) { y--; break; }
     if (ae) { x++; break; }
     if (aw) { x--; break; }
+    const bool ane = av(hn && he, ie + 1);
     if (ane && !is_v_[ie + 1]) { x++; y++; continue; }
+    const bool anw = av(hn && hw, iw + 1);
     if (anw && !is_v_[iw + 1]) { x--; y++; continue; }
+    const bool ase = av(hs && he, ie - 1);
     if (ase && !is_v_[ie - 1]) { x++; y--; continue; }
+    const bool asw = av(hs && hw, iw - 1);
     if (asw && !is_v_[iw - 1]) { x--; y--; continue; }
     if (ane) { x++; y++; break; }
     if (anw) { x--; y++; break; }
@@ -354,8 +408,15 @@ void Contours::split(int e_id, size_t p) {
 // (lib_image.hh:1521-1527): split where a point deviates from the chord by
 // more than max(0.05 x chord, 2 px), or where it is seen from either end
 // at more than pi/2 from the chord, at the point farthest from the chord.
+//
+// The reference's angle test, acos(dot / (|a| |r|)) > pi/2 (the double
+// nearest), is the sign of dot here: on the integer grid dot is an exact
+// integer and |a| |r| < 2^33, so a non-zero dot puts the cosine at least
+// 2^-33 from 0, where acos is many roundings away from pi/2 on either
+// side; dot == 0 gives acos(0) = pi/2, not above it; a chord of length 0
+// gives NaN, which never cuts.
 void Contours::subdivide_local() {
-  const double max_angle = (double)1.5707963267948966192313216916397514L, max_dev = 0.05, tol = 2.0;
+  const double max_dev = 0.05, tol = 2.0;
   std::deque<int> q;
   for (size_t e = 0; e < edge.size(); e++) q.push_back((int)e);
   while (!q.empty()) {
@@ -379,9 +440,7 @@ void Contours::subdivide_local() {
       if (!cut) {
         const double px = P[n] / W_, py = P[n] % W_;
         const double ax = px - sx, ay = py - sy, bx = px - ex, by = py - ey;
-        const double a0 = acos((ax * rx + ay * ry) / (sqrt(ax * ax + ay * ay) * len));
-        const double a1 = acos((bx * -rx + by * -ry) / (sqrt(bx * bx + by * by) * len));
-        cut = ((a0 > a1) ? a0 : a1) > max_angle;
+        cut = len > 0 && ((ax * rx + ay * ry) < 0 || (bx * -rx + by * -ry) < 0);
       }
     }
     if (cut) {
@@ -433,12 +492,13 @@ void ref_quicksort(std::vector<int>& a, long lo, long hi, const Cmp& cmp) {
 bool Contours::subdivide_global() {
   // (1) edges joining the same two vertices: split the less straight one
   {
-    auto key_cmp = [&](int a, int b) {
-      const int a0 = std::min(edge[a].vs, edge[a].ve), a1 = std::max(edge[a].vs, edge[a].ve);
-      const int b0 = std::min(edge[b].vs, edge[b].ve), b1 = std::max(edge[b].vs, edge[b].ve);
-      if (a0 != b0) return a0 < b0 ? -1 : 1;
-      return a1 < b1 ? -1 : (a1 > b1 ? 1 : 0);
-    };
+    // each edge's (smaller, larger) end vertex as one number, taken before
+    // the splits below: an edge split there is not compared again
+    std::vector<uint64_t> key(edge.size());
+    for (size_t e = 0; e < edge.size(); e++)
+      key[e] = ((uint64_t)(uint32_t)std::min(edge[e].vs, edge[e].ve) << 32) |
+               (uint32_t)std::max(edge[e].vs, edge[e].ve);
+    auto key_cmp = [&](int a, int b) { return key[a] < key[b] ? -1 : (key[a] > key[b] ? 1 : 0); };
     std::vector<int> order(edge.size());
     for (size_t e = 0; e < edge.size(); e++) order[e] = (int)e;
     if (order.size() > 1) ref_quicksort(order, 0, (long)order.size() - 1, key_cmp);
@@ -489,13 +549,19 @@ bool Contours::subdivide_global() {
       if (split_prev) prev = cur;
     }
   }
-  // (2) until no chord crosses another chord's interior
+  // (2) until no chord crosses another chord's interior.  After the first
+  // round only pairs with a chord split or added in the previous round, or
+  // with a vertex added there, are tested: every other pair was tested with
+  // the same end points and gave no split (a finding splits one of its two).
+  std::vector<uint8_t> dirty(edge.size(), 1);  // chords changed since the last round
+  size_t v_new = 0;                           // vertices from v_new on were added since the last round
   for (int round = 0;; round++) {
     if (round > 100000) return false;
     const size_t ne = edge.size(), nv = vert.size();
     // cells of 8 x 8 pixels (CSR); a chord is listed in every cell its bounding box covers
     const int CS = 8, GX = (H_ + CS - 1) / CS, GY = (W_ + CS - 1) / CS;
     std::vector<int> cstart((size_t)GX * GY + 1, 0), cell_items;
+    std::vector<uint8_t> cell_dirty((size_t)GX * GY, 0);  // a changed chord covers the cell
     for (int pass = 0; pass < 2; pass++) {
       if (pass == 1) {
         for (size_t c = 0; c < (size_t)GX * GY; c++) cstart[c + 1] += cstart[c];
@@ -508,6 +574,7 @@ bool Contours::subdivide_global() {
             const size_t c = (size_t)cx * GY + cy;
             if (pass == 0) cstart[c + 1]++;
             else cell_items[cstart[c]++] = (int)e;
+            if (pass == 0 && dirty[e]) cell_dirty[c] = 1;
           }
       }
       if (pass == 1)  // restore the starts
@@ -528,8 +595,11 @@ bool Contours::subdivide_global() {
       for (size_t v = nv * t / nt; v < nv * (t + 1) / nt; v++) {
         const i64 px = vert[v].x, py = vert[v].y;
         const size_t cv = (size_t)(px / CS) * GY + py / CS;
+        const bool v_changed = v >= v_new;
+        if (!v_changed && !cell_dirty[cv]) continue;
         for (const int* it = cell_begin(cv); it != cell_end(cv); ++it) {
           const int e = *it;
+          if (!v_changed && !dirty[e]) continue;
           const int a = edge[e].vs, b = edge[e].ve;
           if (a == (int)v || b == (int)v) continue;
           const i64 ax = vert[a].x, ay = vert[a].y, bx = vert[b].x, by = vert[b].y;
@@ -547,10 +617,12 @@ bool Contours::subdivide_global() {
       // A pair is tested in the cell holding the corner of its boxes' overlap.
       for (int cx = GX * t / nt; cx < GX * (t + 1) / nt; cx++)
         for (int cy = 0; cy < GY; cy++) {
+          if (!cell_dirty[(size_t)cx * GY + cy]) continue;
           const int* c = cell_begin((size_t)cx * GY + cy);
           const size_t csz = (size_t)(cell_end((size_t)cx * GY + cy) - c);
           for (size_t i = 0; i < csz; i++)
             for (size_t j = i + 1; j < csz; j++) {
+              if (!dirty[c[i]] && !dirty[c[j]]) continue;
               const int s = std::min(c[i], c[j]), tt = std::max(c[i], c[j]);
               const Vert &a0 = vert[edge[s].vs], &a1 = vert[edge[s].ve];
               const Vert &b0 = vert[edge[tt].vs], &b1 = vert[edge[tt].ve];
@@ -618,11 +690,15 @@ bool Contours::subdivide_global() {
         for (size_t e = 0; e < ne; e++) mark[e] |= marks[t][e];
     }
     if (!found) break;
+    std::fill(dirty.begin(), dirty.end(), 0);
     for (size_t e = 0; e < ne; e++) {
       if (!mark[e]) continue;
       if (edge[e].px.empty()) return false;
       split((int)e, farthest(edge[e]));
+      dirty[e] = 1;
     }
+    dirty.resize(edge.size(), 1);  // the split-off tails
+    v_new = nv;
   }
   return true;
 }
