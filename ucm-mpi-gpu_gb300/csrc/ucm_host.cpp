@@ -1102,7 +1102,8 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
   std::vector<int> up(n);  // union-find; a root is a live region, its id the father's
   for (int c = 0; c < n; c++) up[c] = c;
   // entries of merged-away regions never pass the label check; they are
-  // dropped from the queue in bulk once they make up about half of it.
+  // dropped from the queue in bulk once they make up a quarter to a half of
+  // it.
   // qcnt: queue entries naming each region; dead: sum over entries of their
   // merged-away regions (between 1x and 2x the dead entries)
   std::vector<int32_t> qcnt(n, 0);
@@ -1226,7 +1227,7 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
       const double d = f.energy();
       if (!(f.pushed == d && f.first == k)) push(kp.second, d, k, father);
     }
-    if (dead >= Q.size() && Q.size() >= 1024) {
+    if (2 * dead >= Q.size() && Q.size() >= 1024) {
       Q.filter([&](const Entry& e) {
         const int a = (int)(e.lo >> 32), b = a ^ pxor[(uint32_t)e.lo];
         if (up[a] == a && up[b] == b) return true;
