@@ -252,18 +252,7 @@ extern "C" gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widt
   // host: mean-boundary merge, calibration, output grid, one image per thread
   const auto t3 = std::chrono::steady_clock::now();
   ctx_parallel_for(ctx, ni, [&](int i) {
-    const size_t G2 = g2[i + 1] - g2[i];
-    std::vector<double> um(double_size ? 0 : G2);
-    double* full = double_size ? ucm_out[i] : um.data();  // the doubled grid is the caller's buffer where asked
-    ucm::mean_pb_merge(w2.data() + g2[i], lab.data() + pix[i], H[i], W[i], full);
-    ucm::normalize(full, G2);
-    if (!double_size) {
-      const int GW = 2 * W[i] + 1;
-      double* o = ucm_out[i];
-      for (int r = 0; r <= H[i]; r++)
-        for (int c = 0; c <= W[i]; c++)
-          o[(size_t)r * (W[i] + 1) + c] = (r < H[i] && c < W[i]) ? um[(size_t)(2 * r + 2) * GW + 2 * c + 2] : 0.0;
-    }
+    ucm::mean_pb_ucm(w2.data() + g2[i], lab.data() + pix[i], H[i], W[i], !double_size, ucm_out[i]);
   });
   const double ms_merge = ms_since(t3);
   u.H = H;

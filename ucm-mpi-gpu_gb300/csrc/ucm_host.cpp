@@ -971,18 +971,22 @@ class Queue {
 // or label check), so only pairs whose energy changed (the son's former
 // neighbours) or whose last entry had the other order are pushed; the pop
 // order, and so every merge, is the reference's.
+//
+// Out: the grid index of every boundary element, in row-major order, and
+// the value it takes (elements are the only non-zero points before
+// CompleteContourMap).
 template <class Real>
-static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double* ucm) {
-  const int GW = 2 * W + 1, GH = 2 * H + 1;
+static void merge_impl(const Real* lb, const int32_t* part, int H, int W, std::vector<int32_t>& ec,
+                       std::vector<double>& eval) {
+  const int GW = 2 * W + 1;
+  ec.clear();
+  eval.clear();
   int n = 0;
   for (size_t p = 0; p < (size_t)H * W; p++) n = std::max(n, part[p] + 1);
-  if (n <= 0) {
-    memset(ucm, 0, sizeof(double) * (size_t)GH * GW);
-    return;
-  }
+  if (n <= 0) return;
   // boundary elements in row-major grid order: regions (a < b), grid index,
   // grid column and strength
-  std::vector<int32_t> ea, eb, ec, ecol;
+  std::vector<int32_t> ea, eb, ecol;
   std::vector<double> ev;
   {
     size_t cnt = 0;
@@ -1250,25 +1254,72 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
   }
   for (Pair& pr : P)  // boundaries never closed (a split adjacency graph)
     if (pr.head >= 0) close(pr, -INFINITY);
-  // the map row by row: zeros, then each element raised once to its
-  // segment's value; then CompleteContourMap on the even rows: every
-  // even-even point takes the largest of its four neighbours (from 0)
-  int32_t e = 0;
-  auto fill_row = [&](int r) {
-    double* out = ucm + (size_t)r * GW;
-    memset(out, 0, sizeof(double) * GW);
-    const int32_t end = (r + 1) * GW;
-    for (; e < ne && ec[e] < end; e++) {
-      const double v = sval[seg[e]];
-      if (v > 0.0) ucm[ec[e]] = v;
+  eval.resize(ne);
+  for (int32_t e = 0; e < ne; e++) eval[e] = sval[seg[e]];
+}
+
+// NormalizeOutput's calibration (contours2ucm.cpp:191-249) of one value:
+// logistic, rescaled and clipped to [0, 1].  Most of the grid is 0 and
+// boundary runs repeat one value, so a value equal to the previous one
+// reuses its result (the same arithmetic either way).
+class Calibrate {
+ public:
+  Calibrate() : f0_(f(0.0)), last_in_(0.0), last_out_(f0_) {}
+  double operator()(double x) {
+    if (x == 0.0) return f0_;
+    if (x != last_in_) {
+      last_in_ = x;
+      last_out_ = f(x);
     }
+    return last_out_;
+  }
+
+ private:
+  static double f(double x) {
+    const double z = 0.0 + 1.0 * -2.7487 + x * 11.1189;
+    double v = 1.0 / (1.0 + exp(-z));
+    v = (v - 0.0602) / (1.0 - 0.0602);
+    return std::min(1.0, std::max(0.0, v));
+  }
+  double f0_, last_in_, last_out_;
+};
+
+enum MapForm { kRaw, kCalibrated, kCalibratedHalf };
+
+// The map from the merge's element values, row by row: zeros, each element
+// raised once (every element starts at 0), then CompleteContourMap on the
+// even rows: every even-even point takes the largest of its four neighbours
+// (from 0).  kRaw and kCalibrated write the (2H+1) x (2W+1) grid, the
+// latter calibrated; kCalibratedHalf writes Contours2Ucm's (H+1) x (W+1)
+// output (contours2ucm.cpp:476-486): calibrated point (2r+2, 2c+2) at
+// (r, c) for r < H, c < W, and 0 in the last row and column.  That form
+// keeps three grid rows at a time.
+static void write_map(const std::vector<int32_t>& ec, const std::vector<double>& eval, int H, int W, MapForm form,
+                      double* out) {
+  const int GW = 2 * W + 1, GH = 2 * H + 1;
+  const bool half = form == kCalibratedHalf;
+  std::vector<double> ring(half ? 3 * (size_t)GW : 0);
+  auto row_at = [&](int r) { return half ? ring.data() + (size_t)(r % 3) * GW : out + (size_t)r * GW; };
+  Calibrate cal;
+  const size_t ne = ec.size();
+  size_t e = 0;
+  auto fill_row = [&](int r) {
+    double* row = row_at(r);
+    memset(row, 0, sizeof(double) * GW);
+    const int32_t base = r * GW, end = base + GW;
+    for (; e < ne && ec[e] < end; e++)
+      if (eval[e] > 0.0) row[ec[e] - base] = eval[e];
+  };
+  auto calibrate_row = [&](int r) {
+    double* row = row_at(r);
+    for (int y = 0; y < GW; y++) row[y] = cal(row[y]);
   };
   for (int x = 0; x < GH; x += 2) {
     fill_row(x);
     if (x + 1 < GH) fill_row(x + 1);
-    double* row = ucm + (size_t)x * GW;
-    const double* below = x + 1 < GH ? row + GW : nullptr;
-    const double* above = x >= 1 ? row - GW : nullptr;
+    double* row = row_at(x);
+    const double* below = x + 1 < GH ? row_at(x + 1) : nullptr;
+    const double* above = x >= 1 ? row_at(x - 1) : nullptr;
     for (int y = 0; y < GW; y += 2) {
       double m = 0.0;
       if (below && m < below[y]) m = below[y];
@@ -1277,43 +1328,38 @@ static void merge_impl(const Real* lb, const int32_t* part, int H, int W, double
       if (y >= 1 && m < row[y - 1]) m = row[y - 1];
       row[y] = m;
     }
+    // rows x - 1 and x are final: no later step reads them
+    if (form == kCalibrated) {
+      if (x >= 1) calibrate_row(x - 1);
+      calibrate_row(x);
+    } else if (half && x >= 2) {
+      double* o = out + (size_t)(x / 2 - 1) * (W + 1);
+      for (int c = 0; c < W; c++) o[c] = cal(row[2 * c + 2]);
+      o[W] = 0.0;
+    }
   }
+  if (half)
+    for (int c = 0; c <= W; c++) out[(size_t)H * (W + 1) + c] = 0.0;
 }
 
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm) {
-  merge_impl(lb, part, H, W, ucm);
+  std::vector<int32_t> ec;
+  std::vector<double> ev;
+  merge_impl(lb, part, H, W, ec, ev);
+  write_map(ec, ev, H, W, kRaw, ucm);
 }
 
-// the same on float strengths (as the device grid holds them; widened exactly)
-void mean_pb_merge(const float* lb, const int32_t* part, int H, int W, double* ucm) {
-  merge_impl(lb, part, H, W, ucm);
+void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out) {
+  std::vector<int32_t> ec;
+  std::vector<double> ev;
+  merge_impl(lb, part, H, W, ec, ev);
+  write_map(ec, ev, H, W, half ? kCalibratedHalf : kCalibrated, out);
 }
 
-// NormalizeOutput (contours2ucm.cpp:191-249): logistic calibration of the
-// mean boundary strength, rescaled and clipped to [0, 1].
-// Most of the grid is 0 and boundary runs repeat one value, so a value
-// equal to the previous one reuses its result (the same arithmetic either way).
+// NormalizeOutput over a whole map
 void normalize(double* u, size_t n) {
-  auto f = [](double x) {
-    const double z = 0.0 + 1.0 * -2.7487 + x * 11.1189;
-    double v = 1.0 / (1.0 + exp(-z));
-    v = (v - 0.0602) / (1.0 - 0.0602);
-    return std::min(1.0, std::max(0.0, v));
-  };
-  const double f0 = f(0.0);
-  double last_in = 0.0, last_out = f0;
-  for (size_t i = 0; i < n; i++) {
-    const double x = u[i];
-    if (x == 0.0) {
-      u[i] = f0;
-    } else if (x == last_in) {
-      u[i] = last_out;
-    } else {
-      last_in = x;
-      last_out = f(x);
-      u[i] = last_out;
-    }
-  }
+  Calibrate cal;
+  for (size_t i = 0; i < n; i++) u[i] = cal(u[i]);
 }
 
 }  // namespace ucm

@@ -21,8 +21,11 @@ uint32_t components8(const uint8_t* bw, int H, int W, std::vector<uint32_t>& lab
 using ParFor = std::function<void(int, const std::function<void(int)>&)>;
 bool fit_contours(const uint8_t* bw, int H, int W, FitResult& out, const ParFor* par = nullptr);
 int edge_orientation(int x1, int y1, int x2, int y2);
+// UcmMeanPb: the (2H+1) x (2W+1) map before calibration
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm);
-void mean_pb_merge(const float* lb, const int32_t* part, int H, int W, double* ucm);
+// the same on float strengths, calibrated (NormalizeOutput): the doubled
+// grid, or with half Contours2Ucm's (H+1) x (W+1) output
+void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out);
 void normalize(double* u, size_t n);
 
 }  // namespace ucm
