@@ -36,7 +36,7 @@ typedef enum {
   GPB_ERR_NOMEM = 3,     /* device or host allocation failed                     */
   GPB_ERR_NOCONV = 4,    /* the eigensolver hit its matvec cap                   */
   GPB_ERR_TIMEOUT = 5,   /* a bounded device wait gave up                        */
-  GPB_ERR_INTERNAL = 6,
+  GPB_ERR_INTERNAL = 6,  /* an unexpected host exception; the message says more  */
   GPB_ERR_TOO_LARGE = 7  /* image beyond gpb_texton_labels_static's fixed scratch */
 } gpb_status;
 
@@ -300,19 +300,22 @@ gpb_status gpb_ucm_fetch(gpb_ctx* ctx, size_t image, int what, void* host, size_
 
 /* The host stages, usable without a device.
  * gpb_ucm_fit_contours: fit_contour (src/fit_contour.cpp) of a 0/1 map of
- *   watershed arcs, row-major height x width.  Vertices as (row, column)
- *   pairs, edges as vertex-id pairs, each edge's interior pixels (row,
- *   column) in off[e] .. off[e+1]; completion edges are not produced.
- *   Returns the number of edges, -1 when a capacity is too small, -2 when
- *   the chords cannot be made consistent (the reference then returns no
- *   contours).
+ *   watershed arcs, row-major height x width (fewer than 2^31 pixels).
+ *   Vertices as (row, column) pairs, edges as vertex-id pairs, each edge's
+ *   interior pixels (row, column) in off[e] .. off[e+1]; completion edges
+ *   are not produced.  Returns the number of edges, -1 for a bad argument
+ *   or a capacity that is too small, -2 when the chords cannot be made
+ *   consistent (the reference then returns no contours), -3 when host
+ *   memory runs out.
  * gpb_ucm_mean_pb: UcmMeanPb (src/ucm_mean_pb.cpp:402-449): the
- *   (2H+1) x (2W+1) mean-boundary map from ws_wt2 and the pixels' region
- *   ids (0-based; negative ids are skipped), all row-major.
+ *   (2H+1) x (2W+1) mean-boundary map (fewer than 2^31 points) from ws_wt2
+ *   and the pixels' region ids (0-based; negative ids are skipped), all
+ *   row-major.  GPB_ERR_NOMEM when host memory runs out.
  * gpb_ucm_labels_at_scale: UCM_generator::generateLabelsAtScaleK
- *   (src/UCMgenerator.cpp:120-161): regions of the doubled-grid map at
- *   threshold k, labels (0-based) of the height x width pixels; returns the
- *   number of regions. */
+ *   (src/UCMgenerator.cpp:120-161): regions of the doubled-grid map (fewer
+ *   than 2^31 points) at threshold k, labels (0-based) of the height x width
+ *   pixels; returns the number of regions, -1 for a bad argument or when
+ *   host memory runs out. */
 int32_t gpb_ucm_fit_contours(const uint8_t* bw, uint32_t width, uint32_t height, int32_t cap_vertices,
                              int32_t cap_edges, int32_t cap_pixels, int32_t* n_vertices, int32_t* vertices,
                              int32_t* edges, int32_t* off, int32_t* pixels);

@@ -199,9 +199,14 @@ def test_merge_layouts_against_reference(ref, layout, strength):
     assert np.array_equal(gpb.ucm_mean_pb(w2, lab), u)
 
 
-def test_merge_rejects_grids_beyond_32_bit_indices():
+def test_host_stages_reject_sizes_beyond_32_bit_indices():
+    """the checks come before any input is read, so one-element arrays stand in"""
     import gpb
     L = gpb._lib()
     one = np.zeros(1)
     lab = np.zeros(1, np.int32)
     assert L.gpb_ucm_mean_pb(one.ctypes.data, lab.ctypes.data, 40000, 40000, one.ctypes.data) == gpb.GPB_ERR_ARG
+    assert L.gpb_ucm_labels_at_scale(one.ctypes.data, 40000, 40000, 0.5, lab.ctypes.data) == -1
+    bw, i32 = np.zeros(1, np.uint8), np.zeros(4, np.int32)
+    assert L.gpb_ucm_fit_contours(bw.ctypes.data, 50000, 50000, 1, 1, 1, i32.ctypes.data, i32.ctypes.data,
+                                  i32.ctypes.data, i32.ctypes.data, i32.ctypes.data) == -1

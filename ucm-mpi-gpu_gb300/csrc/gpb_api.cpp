@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <exception>
 #include <functional>
 #include <map>
 #include <memory>
@@ -139,7 +140,8 @@ struct Buf {
 // A fixed set of host threads for the per-patch dense work between device
 // phases (the 32 x 32 eigenproblems of the block solver): run(n, f) calls
 // f(0..n-1) on the workers and the calling thread and returns when all are
-// done.
+// done.  The first exception that an f(i) throws is thrown again by run once
+// all are done.
 class HostPool {
  public:
   explicit HostPool(unsigned nthreads) {
@@ -171,11 +173,24 @@ class HostPool {
     std::unique_lock<std::mutex> lk(mu_);
     done_.wait(lk, [this] { return busy_ == 0; });
     f_ = nullptr;
+    if (err_) {
+      std::exception_ptr e = err_;
+      err_ = nullptr;
+      lk.unlock();
+      std::rethrow_exception(e);
+    }
   }
 
  private:
   void drain() {
-    for (int i; (i = next_.fetch_add(1)) < n_;) (*f_)(i);
+    for (int i; (i = next_.fetch_add(1)) < n_;) {
+      try {
+        (*f_)(i);
+      } catch (...) {
+        std::lock_guard<std::mutex> lk(err_mu_);
+        if (!err_) err_ = std::current_exception();
+      }
+    }
   }
   void work() {
     uint64_t seen = 0;
@@ -192,7 +207,8 @@ class HostPool {
     }
   }
   std::vector<std::thread> th_;
-  std::mutex mu_;
+  std::mutex mu_, err_mu_;
+  std::exception_ptr err_;
   std::condition_variable cv_, done_;
   const std::function<void(int)>* f_ = nullptr;
   std::atomic<int> next_{0};
@@ -372,79 +388,88 @@ extern "C" int gpb_device_count(void) {
 extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
   if (!out) return GPB_ERR_ARG;
   *out = nullptr;
-  gpb_ctx* ctx = new (std::nothrow) gpb_ctx();
-  if (!ctx) return GPB_ERR_NOMEM;
-  if (p) ctx->prm = *p;
-  else gpb_default_params(&ctx->prm);
-  gpb_params& q = ctx->prm;
-  if (q.nvec < 2 || q.nvec > kMaxNvec || q.krylov_dim > kMaxKrylov || q.krylov_keep >= q.krylov_dim ||
-      q.krylov_keep < q.nvec || !(q.eig_tol > 0) || q.eig_mode < GPB_EIG_LANCZOS || q.eig_mode > GPB_EIG_BLOCK ||
-      (q.eig_mode != GPB_EIG_LANCZOS && q.nvec > kBlk) || (q.eig_mode == GPB_EIG_WARM && !(q.warm_tol > 0))) {
-    delete ctx;
-    return GPB_ERR_ARG;
-  }
-  if (q.device >= 0) {
-    if (cudaSetDevice(q.device) != cudaSuccess) {
+  gpb_ctx* ctx = nullptr;
+  try {
+    ctx = new (std::nothrow) gpb_ctx();
+    if (!ctx) return GPB_ERR_NOMEM;
+    if (p) ctx->prm = *p;
+    else gpb_default_params(&ctx->prm);
+    gpb_params& q = ctx->prm;
+    if (q.nvec < 2 || q.nvec > kMaxNvec || q.krylov_dim > kMaxKrylov || q.krylov_keep >= q.krylov_dim ||
+        q.krylov_keep < q.nvec || !(q.eig_tol > 0) || q.eig_mode < GPB_EIG_LANCZOS || q.eig_mode > GPB_EIG_BLOCK ||
+        (q.eig_mode != GPB_EIG_LANCZOS && q.nvec > kBlk) || (q.eig_mode == GPB_EIG_WARM && !(q.warm_tol > 0))) {
+      delete ctx;
+      return GPB_ERR_ARG;
+    }
+    if (q.device >= 0) {
+      if (cudaSetDevice(q.device) != cudaSuccess) {
+        delete ctx;
+        return GPB_ERR_CUDA;
+      }
+    }
+    cudaGetDevice(&ctx->device);
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
       delete ctx;
       return GPB_ERR_CUDA;
     }
-  }
-  cudaGetDevice(&ctx->device);
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
-    delete ctx;
-    return GPB_ERR_CUDA;
-  }
-  for (int i = 0; i < 12; i++) cudaEventCreate(&ctx->ev[i]);
-  {
-    const char* pe = getenv("GPB_PROFILE");
-    ctx->profile = pe && pe[0] == '1';
-    const char* tr = getenv("GPB_TRACE");
-    ctx->trace = tr && tr[0] == '1';
-  }
-  build_tables(ctx->tab, q.compat);
-  cudaStream_t s = ctx->st;
-  ctx->token = g_next_token++;
-  bool loaded;
-  {
-    std::lock_guard<std::mutex> lk(bank_of(ctx->device).mu);
-    loaded = load_tables(ctx) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
-  }
-  if (!loaded) {
-    gpb_destroy(ctx);
-    return GPB_ERR_CUDA;
-  }
-  // global tables: IC paths, FP64 ring coefficients and the offset->ring map
-  size_t nic = ctx->tab.ic.size();
-  std::vector<int> ring_of(2401);
-  {
-    int rid[2 * 24 * 24 + 1];
-    for (int t = 0; t <= 2 * 24 * 24; t++) rid[t] = -1;
-    for (int a = 0; a <= 24; a++)
-      for (int bb = 0; bb <= 24; bb++) rid[a * a + bb * bb] = 0;
-    int nr = 0;
-    for (int t = 0; t <= 2 * 24 * 24; t++)
-      if (rid[t] == 0) rid[t] = nr++;
-    for (int o = 0; o < 2401; o++) {
-      const int dy = o / 49 - 24, dx = o % 49 - 24;
-      ring_of[o] = rid[dy * dy + dx * dx];
+    for (int i = 0; i < 12; i++) cudaEventCreate(&ctx->ev[i]);
+    {
+      const char* pe = getenv("GPB_PROFILE");
+      ctx->profile = pe && pe[0] == '1';
+      const char* tr = getenv("GPB_TRACE");
+      ctx->trace = tr && tr[0] == '1';
     }
-  }
-  if (cudaMalloc(&ctx->d_ic, nic * sizeof(IcPath)) != cudaSuccess ||
-      cudaMalloc(&ctx->d_k32_ring, ctx->tab.k32_ring.size() * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&ctx->d_ring_of, 2401 * sizeof(int)) != cudaSuccess) {
+    build_tables(ctx->tab, q.compat);
+    cudaStream_t s = ctx->st;
+    ctx->token = g_next_token++;
+    bool loaded;
+    {
+      std::lock_guard<std::mutex> lk(bank_of(ctx->device).mu);
+      loaded = load_tables(ctx) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+    }
+    if (!loaded) {
+      gpb_destroy(ctx);
+      return GPB_ERR_CUDA;
+    }
+    // global tables: IC paths, FP64 ring coefficients and the offset->ring map
+    size_t nic = ctx->tab.ic.size();
+    std::vector<int> ring_of(2401);
+    {
+      int rid[2 * 24 * 24 + 1];
+      for (int t = 0; t <= 2 * 24 * 24; t++) rid[t] = -1;
+      for (int a = 0; a <= 24; a++)
+        for (int bb = 0; bb <= 24; bb++) rid[a * a + bb * bb] = 0;
+      int nr = 0;
+      for (int t = 0; t <= 2 * 24 * 24; t++)
+        if (rid[t] == 0) rid[t] = nr++;
+      for (int o = 0; o < 2401; o++) {
+        const int dy = o / 49 - 24, dx = o % 49 - 24;
+        ring_of[o] = rid[dy * dy + dx * dx];
+      }
+    }
+    if (cudaMalloc(&ctx->d_ic, nic * sizeof(IcPath)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_k32_ring, ctx->tab.k32_ring.size() * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_ring_of, 2401 * sizeof(int)) != cudaSuccess) {
+      gpb_destroy(ctx);
+      return GPB_ERR_NOMEM;
+    }
+    cudaMemcpyAsync(ctx->d_ic, ctx->tab.ic.data(), nic * sizeof(IcPath), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ctx->d_k32_ring, ctx->tab.k32_ring.data(), ctx->tab.k32_ring.size() * sizeof(double),
+                    cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ctx->d_ring_of, ring_of.data(), 2401 * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      gpb_destroy(ctx);
+      return GPB_ERR_CUDA;
+    }
+    *out = ctx;
+    return GPB_OK;
+  } catch (const std::bad_alloc&) {  // a host table could not be allocated
     gpb_destroy(ctx);
     return GPB_ERR_NOMEM;
-  }
-  cudaMemcpyAsync(ctx->d_ic, ctx->tab.ic.data(), nic * sizeof(IcPath), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(ctx->d_k32_ring, ctx->tab.k32_ring.data(), ctx->tab.k32_ring.size() * sizeof(double),
-                  cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(ctx->d_ring_of, ring_of.data(), 2401 * sizeof(int), cudaMemcpyHostToDevice, s);
-  if (cudaStreamSynchronize(s) != cudaSuccess) {
+  } catch (...) {
     gpb_destroy(ctx);
-    return GPB_ERR_CUDA;
+    return GPB_ERR_INTERNAL;
   }
-  *out = ctx;
-  return GPB_OK;
 }
 
 extern "C" void gpb_destroy(gpb_ctx* ctx) {
@@ -481,54 +506,58 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
 }
 
 extern "C" gpb_status gpb_set_codebook(gpb_ctx* ctx, const float* cb, int K) {
-  if (!ctx || !cb || K < 1 || K > kMaxCodewords) return GPB_ERR_ARG;
-  cudaSetDevice(ctx->device);
-  ConstBank& bk = bank_of(ctx->device);
-  std::lock_guard<std::mutex> lk(bk.mu);
-  ctx->cb_host.assign(cb, cb + (size_t)kNschmid * K);
-  ctx->K = K;
-  bk.owner = 0;  // reload everything under this context's token
-  if (load_tables(ctx) != cudaSuccess || cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
-  return GPB_OK;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !cb || K < 1 || K > kMaxCodewords) return GPB_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    ConstBank& bk = bank_of(ctx->device);
+    std::lock_guard<std::mutex> lk(bk.mu);
+    ctx->cb_host.assign(cb, cb + (size_t)kNschmid * K);
+    ctx->K = K;
+    bk.owner = 0;  // reload everything under this context's token
+    if (load_tables(ctx) != cudaSuccess || cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
+    return GPB_OK;
+  });
 }
 
 // minimal reader for an OpenCV FileStorage YAML matrix named texton_codebook
 extern "C" gpb_status gpb_load_codebook_yml(gpb_ctx* ctx, const char* path) {
-  if (!ctx || !path) return GPB_ERR_ARG;
-  FILE* f = fopen(path, "rb");
-  if (!f) return GPB_ERR_ARG;
-  std::string s;
-  char buf[4096];
-  size_t n;
-  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
-  fclose(f);
-  size_t at = s.find("texton_codebook");
-  if (at == std::string::npos) return GPB_ERR_ARG;
-  auto num_after = [&](const char* key, size_t from) -> long {
-    size_t k = s.find(key, from);
-    if (k == std::string::npos) return -1;
-    return strtol(s.c_str() + k + strlen(key), nullptr, 10);
-  };
-  const long rows = num_after("rows:", at), cols = num_after("cols:", at);
-  size_t d = s.find("data:", at);
-  if (rows != kNschmid || cols < 1 || cols > kMaxCodewords || d == std::string::npos) return GPB_ERR_ARG;
-  d = s.find('[', d);
-  if (d == std::string::npos) return GPB_ERR_ARG;
-  std::vector<float> v;
-  const char* c = s.c_str() + d + 1;
-  while ((long)v.size() < rows * cols) {
-    char* e;
-    const double x = strtod(c, &e);
-    if (e == c) {
-      if (*c == 0) break;
-      c++;
-      continue;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !path) return GPB_ERR_ARG;
+    FILE* f = fopen(path, "rb");
+    if (!f) return GPB_ERR_ARG;
+    std::string s;
+    char buf[4096];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
+    fclose(f);
+    size_t at = s.find("texton_codebook");
+    if (at == std::string::npos) return GPB_ERR_ARG;
+    auto num_after = [&](const char* key, size_t from) -> long {
+      size_t k = s.find(key, from);
+      if (k == std::string::npos) return -1;
+      return strtol(s.c_str() + k + strlen(key), nullptr, 10);
+    };
+    const long rows = num_after("rows:", at), cols = num_after("cols:", at);
+    size_t d = s.find("data:", at);
+    if (rows != kNschmid || cols < 1 || cols > kMaxCodewords || d == std::string::npos) return GPB_ERR_ARG;
+    d = s.find('[', d);
+    if (d == std::string::npos) return GPB_ERR_ARG;
+    std::vector<float> v;
+    const char* c = s.c_str() + d + 1;
+    while ((long)v.size() < rows * cols) {
+      char* e;
+      const double x = strtod(c, &e);
+      if (e == c) {
+        if (*c == 0) break;
+        c++;
+        continue;
+      }
+      v.push_back((float)x);
+      c = e;
     }
-    v.push_back((float)x);
-    c = e;
-  }
-  if ((long)v.size() != rows * cols) return GPB_ERR_ARG;
-  return gpb_set_codebook(ctx, v.data(), (int)cols);
+    if ((long)v.size() != rows * cols) return GPB_ERR_ARG;
+    return gpb_set_codebook(ctx, v.data(), (int)cols);
+  });
 }
 
 // ------------------------------------------------------------------ batch
@@ -1430,19 +1459,21 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
 }
 
 extern "C" gpb_status gpb_compute_batch(gpb_ctx* ctx, const gpb_patch* patches, size_t n, gpb_result* out) {
-  if (!ctx || !patches || !out || n == 0) return GPB_ERR_ARG;
-  std::vector<uint32_t> ws(n), hs(n);
-  std::vector<const uint32_t*> in(n);
-  std::vector<size_t> stride(n);
-  for (size_t i = 0; i < n; i++) {
-    if (!patches[i].packed_bgr) return GPB_ERR_ARG;
-    ws[i] = patches[i].width;
-    hs[i] = patches[i].height;
-    in[i] = patches[i].packed_bgr;
-    stride[i] = patches[i].stride ? patches[i].stride : patches[i].width;
-  }
-  return run_batch(ctx, n, ws.data(), hs.data(), in.data(), stride.data(), nullptr, nullptr, nullptr, nullptr,
-                   out);
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !patches || !out || n == 0) return GPB_ERR_ARG;
+    std::vector<uint32_t> ws(n), hs(n);
+    std::vector<const uint32_t*> in(n);
+    std::vector<size_t> stride(n);
+    for (size_t i = 0; i < n; i++) {
+      if (!patches[i].packed_bgr) return GPB_ERR_ARG;
+      ws[i] = patches[i].width;
+      hs[i] = patches[i].height;
+      in[i] = patches[i].packed_bgr;
+      stride[i] = patches[i].stride ? patches[i].stride : patches[i].width;
+    }
+    return run_batch(ctx, n, ws.data(), hs.data(), in.data(), stride.data(), nullptr, nullptr, nullptr, nullptr,
+                     out);
+  });
 }
 
 extern "C" gpb_status gpb_compute(gpb_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* packed,
@@ -1464,20 +1495,22 @@ extern "C" gpb_status gpb_compute(gpb_ctx* ctx, uint32_t width, uint32_t height,
 extern "C" gpb_status gpb_compute_batch_device(gpb_ctx* ctx, size_t n, const uint32_t* widths,
                                                const uint32_t* heights, const size_t* offsets,
                                                const uint32_t* d_packed, float* d_nmax, float* d_orient) {
-  if (!ctx || !widths || !heights || !offsets || !d_packed || !d_nmax || !d_orient || n == 0) return GPB_ERR_ARG;
-  // outputs are written in the library's compact layout, then moved to the
-  // caller's offsets when they differ
-  gpb_status s = run_batch(ctx, n, widths, heights, nullptr, nullptr, d_packed, offsets, nullptr, nullptr, nullptr);
-  if (s != GPB_OK && s != GPB_ERR_NOCONV) return s;
-  for (size_t i = 0; i < n; i++) {
-    const PatchDev& P = ctx->patches[i];
-    CK(cudaMemcpyAsync(d_nmax + offsets[i], ctx->b.nmax + P.pix, (size_t)P.N * sizeof(float),
-                       cudaMemcpyDeviceToDevice, ctx->st));
-    CK(cudaMemcpyAsync(d_orient + 8 * offsets[i], ctx->b.orient + 8 * P.pix, 8 * (size_t)P.N * sizeof(float),
-                       cudaMemcpyDeviceToDevice, ctx->st));
-  }
-  CK(cudaStreamSynchronize(ctx->st));
-  return s;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !widths || !heights || !offsets || !d_packed || !d_nmax || !d_orient || n == 0) return GPB_ERR_ARG;
+    // outputs are written in the library's compact layout, then moved to the
+    // caller's offsets when they differ
+    gpb_status s = run_batch(ctx, n, widths, heights, nullptr, nullptr, d_packed, offsets, nullptr, nullptr, nullptr);
+    if (s != GPB_OK && s != GPB_ERR_NOCONV) return s;
+    for (size_t i = 0; i < n; i++) {
+      const PatchDev& P = ctx->patches[i];
+      CK(cudaMemcpyAsync(d_nmax + offsets[i], ctx->b.nmax + P.pix, (size_t)P.N * sizeof(float),
+                         cudaMemcpyDeviceToDevice, ctx->st));
+      CK(cudaMemcpyAsync(d_orient + 8 * offsets[i], ctx->b.orient + 8 * P.pix, 8 * (size_t)P.N * sizeof(float),
+                         cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    return s;
+  });
 }
 
 extern "C" gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st) {
@@ -1487,82 +1520,84 @@ extern "C" gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st) {
 }
 
 extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst, size_t bytes) {
-  if (!ctx || !dst || patch >= ctx->patches.size()) return GPB_ERR_ARG;
-  cudaSetDevice(ctx->device);
-  const PatchDev& P = ctx->patches[patch];
-  const size_t N = P.N;
-  Buf& b = ctx->b;
-  const int nvec = ctx->prm.nvec;
-  auto need = [&](size_t x) { return bytes >= x; };
-  cudaError_t e = cudaSuccess;
-  switch (stage) {
-    case GPB_STAGE_TEXTON:
-    case GPB_STAGE_LABBINS: {
-      std::vector<uint32_t> v(N);
-      e = cudaMemcpy(v.data(), b.lab4 + P.pix, N * 4, cudaMemcpyDeviceToHost);
-      uint8_t* o = (uint8_t*)dst;
-      if (stage == GPB_STAGE_TEXTON) {
-        if (!need(N)) return GPB_ERR_ARG;
-        for (size_t i = 0; i < N; i++) o[i] = (uint8_t)(v[i] >> 24);
-      } else {
-        if (!need(3 * N)) return GPB_ERR_ARG;
-        for (int c = 0; c < 3; c++)
-          for (size_t i = 0; i < N; i++) o[c * N + i] = (uint8_t)((v[i] >> (8 * c)) & 255);
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !dst || patch >= ctx->patches.size()) return GPB_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const PatchDev& P = ctx->patches[patch];
+    const size_t N = P.N;
+    Buf& b = ctx->b;
+    const int nvec = ctx->prm.nvec;
+    auto need = [&](size_t x) { return bytes >= x; };
+    cudaError_t e = cudaSuccess;
+    switch (stage) {
+      case GPB_STAGE_TEXTON:
+      case GPB_STAGE_LABBINS: {
+        std::vector<uint32_t> v(N);
+        e = cudaMemcpy(v.data(), b.lab4 + P.pix, N * 4, cudaMemcpyDeviceToHost);
+        uint8_t* o = (uint8_t*)dst;
+        if (stage == GPB_STAGE_TEXTON) {
+          if (!need(N)) return GPB_ERR_ARG;
+          for (size_t i = 0; i < N; i++) o[i] = (uint8_t)(v[i] >> 24);
+        } else {
+          if (!need(3 * N)) return GPB_ERR_ARG;
+          for (int c = 0; c < 3; c++)
+            for (size_t i = 0; i < N; i++) o[c * N + i] = (uint8_t)((v[i] >> (8 * c)) & 255);
+        }
+        break;
       }
-      break;
+      case GPB_STAGE_MPB_O:
+        if (!need(8 * N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.mpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_MPB:
+        if (!need(N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.mpb + P.pix, N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_W:
+        if (!b.wfull || !need(81 * N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.wfull + 81 * P.pix, 81 * N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_EVALS:
+        if (!need((size_t)nvec * 4) || ctx->evals_host.size() < (patch + 1) * nvec) return GPB_ERR_ARG;
+        memcpy(dst, ctx->evals_host.data() + patch * nvec, (size_t)nvec * 4);
+        break;
+      case GPB_STAGE_EVECS:
+        if (!need((size_t)nvec * N * 4)) return GPB_ERR_ARG;
+        for (int i = 0; i < nvec && e == cudaSuccess; i++)
+          e = cudaMemcpy((float*)dst + i * N, b.evec + (size_t)i * ctx->lvec + P.vec, N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_SPB:
+        if (!b.spb || !need(8 * N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.spb + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_CUES:
+        if (!b.raw || !need(96 * N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.raw + 96 * P.pix, 96 * N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_GPB_O:
+        if (!b.gpbo || !need(8 * N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.gpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
+        break;
+      case GPB_STAGE_WARM0: {  // first 9 columns of the captured start block, pixel-major
+        if (!ctx->d_wn_x0 || !need(N * kWnOut * 4)) return GPB_ERR_ARG;
+        std::vector<float> blk(N * kBlk);
+        e = cudaMemcpy(blk.data(), ctx->d_wn_x0 + (size_t)P.vec * kBlk, N * kBlk * 4, cudaMemcpyDeviceToHost);
+        float* o = (float*)dst;
+        for (size_t i = 0; i < N; i++)
+          for (int c = 0; c < kWnOut; c++) o[i * kWnOut + c] = blk[i * kBlk + c];
+        break;
+      }
+      case GPB_STAGE_COUNTS: {
+        const size_t per = (size_t)kNannulus * 4 * 32 * 32;
+        if (!b.counts || !need(per * N)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.counts + per * P.pix, per * N, cudaMemcpyDeviceToHost);
+        break;
+      }
+      default:
+        return GPB_ERR_ARG;
     }
-    case GPB_STAGE_MPB_O:
-      if (!need(8 * N * 4)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.mpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_MPB:
-      if (!need(N * 4)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.mpb + P.pix, N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_W:
-      if (!b.wfull || !need(81 * N * 4)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.wfull + 81 * P.pix, 81 * N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_EVALS:
-      if (!need((size_t)nvec * 4) || ctx->evals_host.size() < (patch + 1) * nvec) return GPB_ERR_ARG;
-      memcpy(dst, ctx->evals_host.data() + patch * nvec, (size_t)nvec * 4);
-      break;
-    case GPB_STAGE_EVECS:
-      if (!need((size_t)nvec * N * 4)) return GPB_ERR_ARG;
-      for (int i = 0; i < nvec && e == cudaSuccess; i++)
-        e = cudaMemcpy((float*)dst + i * N, b.evec + (size_t)i * ctx->lvec + P.vec, N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_SPB:
-      if (!b.spb || !need(8 * N * 4)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.spb + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_CUES:
-      if (!b.raw || !need(96 * N * 4)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.raw + 96 * P.pix, 96 * N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_GPB_O:
-      if (!b.gpbo || !need(8 * N * 4)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.gpbo + 8 * P.pix, 8 * N * 4, cudaMemcpyDeviceToHost);
-      break;
-    case GPB_STAGE_WARM0: {  // first 9 columns of the captured start block, pixel-major
-      if (!ctx->d_wn_x0 || !need(N * kWnOut * 4)) return GPB_ERR_ARG;
-      std::vector<float> blk(N * kBlk);
-      e = cudaMemcpy(blk.data(), ctx->d_wn_x0 + (size_t)P.vec * kBlk, N * kBlk * 4, cudaMemcpyDeviceToHost);
-      float* o = (float*)dst;
-      for (size_t i = 0; i < N; i++)
-        for (int c = 0; c < kWnOut; c++) o[i * kWnOut + c] = blk[i * kBlk + c];
-      break;
-    }
-    case GPB_STAGE_COUNTS: {
-      const size_t per = (size_t)kNannulus * 4 * 32 * 32;
-      if (!b.counts || !need(per * N)) return GPB_ERR_ARG;
-      e = cudaMemcpy(dst, b.counts + per * P.pix, per * N, cudaMemcpyDeviceToHost);
-      break;
-    }
-    default:
-      return GPB_ERR_ARG;
-  }
-  return e == cudaSuccess ? GPB_OK : GPB_ERR_CUDA;
+    return e == cudaSuccess ? GPB_OK : GPB_ERR_CUDA;
+  });
 }
 
 // Whole-image planes from the last batch's patches (Pieces2Gpb,
@@ -1570,72 +1605,76 @@ extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst
 extern "C" gpb_status gpb_stitch_device(gpb_ctx* ctx, int mode, uint32_t width, uint32_t height,
                                         const gpb_place* places, size_t n, int ramp, float* d_nmax,
                                         float* d_orient) {
-  if (!ctx || !places || !d_nmax || !d_orient || width == 0 || height == 0) return GPB_ERR_ARG;
-  if (mode < GPB_STITCH_LAST || mode > GPB_STITCH_BLEND) return GPB_ERR_ARG;
-  if (n == 0 || n != ctx->patches.size()) {
-    ctx->last_error = "place count differs from the last batch";
-    return GPB_ERR_ARG;
-  }
-  for (size_t i = 0; i < n; i++) {
-    const gpb_place& q = places[i];
-    const PatchDev& P = ctx->patches[i];
-    if (q.ix < 0 || q.iy < 0 || q.iw < 0 || q.ih < 0 || q.ix + q.iw > P.W || q.iy + q.ih > P.H) return GPB_ERR_ARG;
-  }
-  CK(cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->st;
-  Buf& b = ctx->b;
-  const int colmajor = ctx->prm.compat == GPB_COMPAT_DAMASCENE;
-  const long long plane = (long long)width * height;
-  if (mode == GPB_STITCH_BLEND) {
-    CK(grow(b.stitch, b.c_stitch, 10 * (size_t)plane));
-    CK(cudaMemsetAsync(b.stitch, 0, 10 * (size_t)plane * sizeof(float), s));
-  }
-  const float rmp = (float)(ramp > 0 ? ramp : 10);
-  for (size_t i = 0; i < n; i++) {
-    const gpb_place& q = places[i];
-    const PatchDev& P = ctx->patches[i];
-    StitchBox bx;
-    bx.ox = q.x0;
-    bx.oy = q.y0;
-    if (mode == GPB_STITCH_INTERIOR) {
-      bx.x = q.ix;
-      bx.y = q.iy;
-      bx.w = q.iw;
-      bx.h = q.ih;
-    } else {
-      bx.x = 0;
-      bx.y = 0;
-      bx.w = P.W;
-      bx.h = P.H;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !places || !d_nmax || !d_orient || width == 0 || height == 0) return GPB_ERR_ARG;
+    if (mode < GPB_STITCH_LAST || mode > GPB_STITCH_BLEND) return GPB_ERR_ARG;
+    if (n == 0 || n != ctx->patches.size()) {
+      ctx->last_error = "place count differs from the last batch";
+      return GPB_ERR_ARG;
     }
-    if (mode == GPB_STITCH_BLEND)
-      CK(launch_stitch_acc(b.patches, (int)i, P.N, b.nmax, b.orient, colmajor, bx, (int)width, (int)height, rmp,
-                           b.stitch, s));
-    else
-      CK(launch_stitch_copy(b.patches, (int)i, b.nmax, b.orient, colmajor, bx, (int)width, (int)height, d_nmax,
-                            d_orient, s));
-  }
-  if (mode == GPB_STITCH_BLEND) CK(launch_stitch_norm(b.stitch, plane, d_nmax, d_orient, s));
-  CK(cudaStreamSynchronize(s));
-  return GPB_OK;
+    for (size_t i = 0; i < n; i++) {
+      const gpb_place& q = places[i];
+      const PatchDev& P = ctx->patches[i];
+      if (q.ix < 0 || q.iy < 0 || q.iw < 0 || q.ih < 0 || q.ix + q.iw > P.W || q.iy + q.ih > P.H) return GPB_ERR_ARG;
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->st;
+    Buf& b = ctx->b;
+    const int colmajor = ctx->prm.compat == GPB_COMPAT_DAMASCENE;
+    const long long plane = (long long)width * height;
+    if (mode == GPB_STITCH_BLEND) {
+      CK(grow(b.stitch, b.c_stitch, 10 * (size_t)plane));
+      CK(cudaMemsetAsync(b.stitch, 0, 10 * (size_t)plane * sizeof(float), s));
+    }
+    const float rmp = (float)(ramp > 0 ? ramp : 10);
+    for (size_t i = 0; i < n; i++) {
+      const gpb_place& q = places[i];
+      const PatchDev& P = ctx->patches[i];
+      StitchBox bx;
+      bx.ox = q.x0;
+      bx.oy = q.y0;
+      if (mode == GPB_STITCH_INTERIOR) {
+        bx.x = q.ix;
+        bx.y = q.iy;
+        bx.w = q.iw;
+        bx.h = q.ih;
+      } else {
+        bx.x = 0;
+        bx.y = 0;
+        bx.w = P.W;
+        bx.h = P.H;
+      }
+      if (mode == GPB_STITCH_BLEND)
+        CK(launch_stitch_acc(b.patches, (int)i, P.N, b.nmax, b.orient, colmajor, bx, (int)width, (int)height, rmp,
+                             b.stitch, s));
+      else
+        CK(launch_stitch_copy(b.patches, (int)i, b.nmax, b.orient, colmajor, bx, (int)width, (int)height, d_nmax,
+                              d_orient, s));
+    }
+    if (mode == GPB_STITCH_BLEND) CK(launch_stitch_norm(b.stitch, plane, d_nmax, d_orient, s));
+    CK(cudaStreamSynchronize(s));
+    return GPB_OK;
+  });
 }
 
 // Superpixel descriptors of one patch of the last batch (SPFeatures,
 // src/SPFeatures.cpp:101-114, 260-275, 380-391, on the device)
 extern "C" gpb_status gpb_superpixel_features(gpb_ctx* ctx, size_t patch, const int32_t* d_labels, int32_t n_labels,
                                               int bin_step, int with_textons, double* d_out) {
-  if (!ctx || !d_labels || !d_out || n_labels <= 0 || bin_step < 1 || bin_step > 255) return GPB_ERR_ARG;
-  if (patch >= ctx->patches.size()) return GPB_ERR_ARG;
-  CK(cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->st;
-  Buf& b = ctx->b;
-  const int K = with_textons ? ctx->K : 0, nbins = 255 / bin_step + 1;
-  CK(grow(b.spcount, b.c_spcount, (size_t)n_labels * (K + nbins + 1)));
-  CK(grow(b.spcsum, b.c_spcsum, (size_t)n_labels * 3));
-  CK(launch_sp_features(b.patches, (int)patch, ctx->patches[patch].N, d_labels, n_labels, b.lab4, b.grey, b.packed,
-                        bin_step, K, nbins, b.spcount, b.spcsum, d_out, s));
-  CK(cudaStreamSynchronize(s));
-  return GPB_OK;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || !d_labels || !d_out || n_labels <= 0 || bin_step < 1 || bin_step > 255) return GPB_ERR_ARG;
+    if (patch >= ctx->patches.size()) return GPB_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->st;
+    Buf& b = ctx->b;
+    const int K = with_textons ? ctx->K : 0, nbins = 255 / bin_step + 1;
+    CK(grow(b.spcount, b.c_spcount, (size_t)n_labels * (K + nbins + 1)));
+    CK(grow(b.spcsum, b.c_spcsum, (size_t)n_labels * 3));
+    CK(launch_sp_features(b.patches, (int)patch, ctx->patches[patch].N, d_labels, n_labels, b.lab4, b.grey, b.packed,
+                          bin_step, K, nbins, b.spcount, b.spcsum, d_out, s));
+    CK(cudaStreamSynchronize(s));
+    return GPB_OK;
+  });
 }
 
 // Texton labels of one device-resident image without allocating: the
@@ -1667,7 +1706,12 @@ extern "C" gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uin
 namespace gpb {
 int ctx_device(gpb_ctx* c) { return c->device; }
 cudaStream_t ctx_stream(gpb_ctx* c) { return c->st; }
-void ctx_set_error(gpb_ctx* c, const char* m) { c->last_error = m; }
+void ctx_set_error(gpb_ctx* c, const char* m) {
+  try {
+    c->last_error = m;
+  } catch (...) {  // the message is lost, the status still tells
+  }
+}
 void ctx_parallel_for(gpb_ctx* c, int n, const std::function<void(int)>& f) { c->host_pool().run(n, f); }
 void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*)) {
   c->ucm_free = release;
@@ -1698,40 +1742,42 @@ extern "C" gpb_status gpb_warmnet_capture(gpb_ctx* ctx, int on) {
 extern "C" gpb_status gpb_warmnet_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
                                               const float* d_xt, const float* d_mpb, const float* d_vt,
                                               const float* weights, double* loss, float* grad) {
-  if (!ctx || n == 0 || !widths || !heights || !d_xt || !d_mpb || !d_vt || !weights || !loss || !grad)
-    return GPB_ERR_ARG;
-  CK(cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->st;
-  std::vector<int4> geo(n);
-  long long tot = 0;
-  int max_n = 0;
-  for (size_t i = 0; i < n; i++) {
-    if (widths[i] == 0 || heights[i] == 0) return GPB_ERR_ARG;
-    geo[i] = make_int4((int)widths[i], (int)heights[i], (int)tot, 0);
-    tot += (long long)widths[i] * heights[i];
-    max_n = std::max(max_n, (int)(widths[i] * heights[i]));
-  }
-  if (tot >= (1ll << 31)) return GPB_ERR_ARG;
-  void* buf = nullptr;
-  const size_t bytes = n * sizeof(int4) + kWnParams * 2 * sizeof(float) + sizeof(double);
-  CK(cudaMalloc(&buf, bytes));
-  int4* d_geo = (int4*)buf;
-  float* d_w = (float*)(d_geo + n);
-  float* d_g = d_w + kWnParams;
-  double* d_l = (double*)(((uintptr_t)(d_g + kWnParams) + 7) & ~(uintptr_t)7);
-  cudaError_t e = cudaMemcpyAsync(d_geo, geo.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, weights, kWnParams * sizeof(float), cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_g, 0, kWnParams * sizeof(float), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_l, 0, sizeof(double), s);
-  if (e == cudaSuccess)
-    e = wn_launch_grad(d_geo, (int)n, max_n, d_xt, d_mpb, d_vt, d_w, 1.0f / (float)(tot * kWnOut), d_g, d_l, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(grad, d_g, kWnParams * sizeof(float), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(loss, d_l, sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(buf);
-  if (e != cudaSuccess) {
-    ctx->last_error = cudaGetErrorString(e);
-    return GPB_ERR_CUDA;
-  }
-  return GPB_OK;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx || n == 0 || !widths || !heights || !d_xt || !d_mpb || !d_vt || !weights || !loss || !grad)
+      return GPB_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->st;
+    std::vector<int4> geo(n);
+    long long tot = 0;
+    int max_n = 0;
+    for (size_t i = 0; i < n; i++) {
+      if (widths[i] == 0 || heights[i] == 0) return GPB_ERR_ARG;
+      geo[i] = make_int4((int)widths[i], (int)heights[i], (int)tot, 0);
+      tot += (long long)widths[i] * heights[i];
+      max_n = std::max(max_n, (int)(widths[i] * heights[i]));
+    }
+    if (tot >= (1ll << 31)) return GPB_ERR_ARG;
+    void* buf = nullptr;
+    const size_t bytes = n * sizeof(int4) + kWnParams * 2 * sizeof(float) + sizeof(double);
+    CK(cudaMalloc(&buf, bytes));
+    int4* d_geo = (int4*)buf;
+    float* d_w = (float*)(d_geo + n);
+    float* d_g = d_w + kWnParams;
+    double* d_l = (double*)(((uintptr_t)(d_g + kWnParams) + 7) & ~(uintptr_t)7);
+    cudaError_t e = cudaMemcpyAsync(d_geo, geo.data(), n * sizeof(int4), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, weights, kWnParams * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_g, 0, kWnParams * sizeof(float), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_l, 0, sizeof(double), s);
+    if (e == cudaSuccess)
+      e = wn_launch_grad(d_geo, (int)n, max_n, d_xt, d_mpb, d_vt, d_w, 1.0f / (float)(tot * kWnOut), d_g, d_l, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(grad, d_g, kWnParams * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(loss, d_l, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(buf);
+    if (e != cudaSuccess) {
+      ctx->last_error = cudaGetErrorString(e);
+      return GPB_ERR_CUDA;
+    }
+    return GPB_OK;
+  });
 }

@@ -5,7 +5,10 @@
 #include <stdint.h>
 
 #include <functional>
+#include <new>
 #include <vector>
+
+#include "../../include/gpb.h"
 
 struct gpb_ctx;
 
@@ -94,5 +97,25 @@ cudaStream_t ctx_stream(gpb_ctx* c);
 void ctx_set_error(gpb_ctx* c, const char* m);
 void*& ctx_ucm_state(gpb_ctx* c, void (*release)(void*));
 void ctx_parallel_for(gpb_ctx* c, int n, const std::function<void(int)>& f);  // f(0..n-1) on the host pool
+
+// Runs an entry point's body.  A host exception (an allocation that failed,
+// a thread that could not start) ends the call with a status and a message
+// on the context instead of leaving the C ABI.
+template <class F>
+gpb_status guarded(gpb_ctx* ctx, F&& body) noexcept {
+  const char* what;
+  gpb_status s;
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    what = "host allocation failed";
+    s = GPB_ERR_NOMEM;
+  } catch (...) {
+    what = "host exception";
+    s = GPB_ERR_INTERNAL;
+  }
+  if (ctx) ctx_set_error(ctx, what);
+  return s;
+}
 
 }  // namespace gpb

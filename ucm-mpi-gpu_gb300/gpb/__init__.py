@@ -344,6 +344,8 @@ def ucm_fit_contours(bw):
                                      ed.ctypes.data, off.ctypes.data, px.ctypes.data)
     if ne == -2:
         return None
+    if ne == -3:
+        raise GpbError(GPB_ERR_NOMEM, "gpb_ucm_fit_contours")
     if ne < 0:
         raise GpbError(GPB_ERR_ARG, "gpb_ucm_fit_contours")
     return (vert[:2 * nv[0]].reshape(-1, 2), ed[:2 * ne].reshape(-1, 2), off[:ne + 1],
@@ -366,6 +368,8 @@ def ucm_labels_at_scale(ucm2, k):
     H, W = (u.shape[0] - 1) // 2, (u.shape[1] - 1) // 2
     lab = np.empty((H, W), np.int32)
     n = _lib().gpb_ucm_labels_at_scale(u.ctypes.data, W, H, float(k), lab.ctypes.data)
+    if n < 0:
+        raise GpbError(GPB_ERR_ARG, "gpb_ucm_labels_at_scale")
     return lab, n
 
 
