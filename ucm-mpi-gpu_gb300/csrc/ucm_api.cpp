@@ -253,7 +253,9 @@ extern "C" gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widt
     // host: mean-boundary merge, calibration, output grid, one image per thread
     const auto t3 = std::chrono::steady_clock::now();
     ctx_parallel_for(ctx, ni, [&](int i) {
-      ucm::mean_pb_ucm(w2.data() + g2[i], lab.data() + pix[i], H[i], W[i], !double_size, ucm_out[i]);
+      // one image alone uses the pool inside the merge's setup and output
+      ucm::mean_pb_ucm(w2.data() + g2[i], lab.data() + pix[i], H[i], W[i], !double_size, ucm_out[i],
+                       n == 1 ? &pool : nullptr);
     });
     const double ms_merge = ms_since(t3);
     u.H = H;

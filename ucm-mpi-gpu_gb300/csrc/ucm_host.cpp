@@ -940,6 +940,48 @@ class Queue {
 
 }  // namespace
 
+// Parts of the merge's setup and output split into chunks: run on the host
+// pool when one is given, in order otherwise.  Chunks are processed so that
+// the result does not depend on their number.
+constexpr int kChunks = 16;
+
+static void for_chunks(const ParFor* par, int nt, const std::function<void(int)>& f) {
+  if (par && nt > 1) (*par)(nt, f);
+  else
+    for (int t = 0; t < nt; t++) f(t);
+}
+
+// Stable counting sort of the sequence in[0..ne) (or 0..ne-1 without in) by
+// key[e] < nkey: place(q, e) puts element e at position q.  Each chunk counts
+// its keys; positions are handed out key by key, chunk by chunk, so equal
+// keys keep their order.
+template <class Place>
+static void count_sort(const ParFor* par, int32_t ne, int nkey, const int32_t* key, const int32_t* in, Place place) {
+  const int nt = par ? kChunks : 1;
+  std::vector<int32_t> off((size_t)nt * nkey);
+  auto lo = [&](int t) { return (int32_t)((int64_t)ne * t / nt); };
+  for_chunks(par, nt, [&](int t) {
+    int32_t* h = off.data() + (size_t)t * nkey;
+    std::fill(h, h + nkey, 0);
+    for (int32_t i = lo(t); i < lo(t + 1); i++) h[key[in ? in[i] : i]]++;
+  });
+  int32_t run = 0;
+  for (int k = 0; k < nkey; k++)
+    for (int t = 0; t < nt; t++) {
+      int32_t& o = off[(size_t)t * nkey + k];
+      const int32_t c = o;
+      o = run;
+      run += c;
+    }
+  for_chunks(par, nt, [&](int t) {
+    int32_t* o = off.data() + (size_t)t * nkey;
+    for (int32_t i = lo(t); i < lo(t + 1); i++) {
+      const int32_t e = in ? in[i] : i;
+      place(o[key[e]]++, e);
+    }
+  });
+}
+
 // ComputeUcm + CompleteContourMap (ucm_mean_pb.cpp:230-398) on the
 // (2H+1) x (2W+1) grid, row-major here (the reference stores it
 // column-major; the grid coordinates are the same).  lb: local boundary
@@ -977,80 +1019,78 @@ class Queue {
 // CompleteContourMap).
 template <class Real>
 static void merge_impl(const Real* lb, const int32_t* part, int H, int W, std::vector<int32_t>& ec,
-                       std::vector<double>& eval) {
+                       std::vector<double>& eval, const ParFor* par) {
   const int GW = 2 * W + 1;
   ec.clear();
   eval.clear();
-  int n = 0;
-  for (size_t p = 0; p < (size_t)H * W; p++) n = std::max(n, part[p] + 1);
-  if (n <= 0) return;
   // boundary elements in row-major grid order: regions (a < b), grid index,
-  // grid column and strength
-  std::vector<int32_t> ea, eb, ecol;
-  std::vector<double> ev;
-  {
-    size_t cnt = 0;
-    for (int x = 0; x < H; x++) {
-      const int32_t* row = part + (size_t)x * W;
-      if (x > 0)
-        for (int y = 0; y < W; y++) cnt += row[y - W] != row[y];
-      for (int y = 1; y < W; y++) cnt += row[y - 1] != row[y];
-    }
-    ea.reserve(cnt);
-    eb.reserve(cnt);
-    ec.reserve(cnt);
-    ecol.reserve(cnt);
-    ev.reserve(cnt);
-  }
-  auto emit = [&](int a, int b, int32_t coord, int32_t col) {
-    if (a < 0 || b < 0) return;
-    ea.push_back(std::min(a, b));
-    eb.push_back(std::max(a, b));
-    ec.push_back(coord);
-    ecol.push_back(col);
-    ev.push_back((double)lb[coord]);
-  };
-  for (int x = 0; x < H; x++) {
+  // grid column and strength.  Bands of pixel rows count theirs, then fill
+  // their slices of the arrays.
+  const int nband = par ? std::min(kChunks, H) : 1;
+  auto band_lo = [&](int t) { return (int)((int64_t)H * t / nband); };
+  std::vector<int64_t> bstart(nband + 1, 0);
+  std::vector<int> bmax(nband, 0);
+  // f(a, b, grid index, grid column) for each boundary element of pixel row x
+  auto scan_row = [&](int x, auto&& f) {
     const int32_t* row = part + (size_t)x * W;
     if (x > 0) {  // grid row 2x: (even, odd) points between pixel rows x-1 and x
       const int32_t* above = row - W;
       const int32_t base = 2 * x * GW + 1;
       for (int y = 0; y < W; y++)
-        if (above[y] != row[y]) emit(above[y], row[y], base + 2 * y, 2 * y + 1);
+        if (above[y] != row[y] && above[y] >= 0 && row[y] >= 0) f(above[y], row[y], base + 2 * y, 2 * y + 1);
     }
     const int32_t base = (2 * x + 1) * GW;  // grid row 2x+1: (odd, even) points within pixel row x
     for (int y = 1; y < W; y++)
-      if (row[y - 1] != row[y]) emit(row[y - 1], row[y], base + 2 * y, 2 * y);
+      if (row[y - 1] != row[y] && row[y - 1] >= 0 && row[y] >= 0) f(row[y - 1], row[y], base + 2 * y, 2 * y);
+  };
+  for_chunks(par, nband, [&](int t) {
+    int64_t c = 0;
+    int m = 0;
+    for (int x = band_lo(t); x < band_lo(t + 1); x++) {
+      const int32_t* row = part + (size_t)x * W;
+      for (int y = 0; y < W; y++) m = std::max(m, row[y] + 1);
+      scan_row(x, [&](int, int, int32_t, int32_t) { c++; });
+    }
+    bstart[t + 1] = c;
+    bmax[t] = m;
+  });
+  int n = 0;
+  for (int t = 0; t < nband; t++) {
+    bstart[t + 1] += bstart[t];
+    n = std::max(n, bmax[t]);
   }
-  const int32_t ne = (int32_t)ea.size();
+  if (n <= 0) return;
+  const int32_t ne = (int32_t)bstart[nband];
+  std::vector<int32_t> ea(ne), eb(ne), ecol(ne);
+  std::vector<double> ev(ne);
+  ec.resize(ne);
+  for_chunks(par, nband, [&](int t) {
+    int64_t q = bstart[t];
+    for (int x = band_lo(t); x < band_lo(t + 1); x++)
+      scan_row(x, [&](int a, int b, int32_t coord, int32_t col) {
+        ea[q] = std::min(a, b);
+        eb[q] = std::max(a, b);
+        ec[q] = coord;
+        ecol[q] = col;
+        ev[q] = (double)lb[coord];
+        q++;
+      });
+  });
   // stable counting sorts by grid column, then b, then a: order[i] is the
   // i-th element in (a, b, column-major) order
-  std::vector<int32_t> order(ne), seg(ne), cnt((size_t)std::max(n, GW) + 1);
-  auto count_sort = [&](const std::vector<int32_t>& key, int nkey, const int32_t* in, int32_t* out) {
-    std::fill(cnt.begin(), cnt.begin() + nkey + 1, 0);
-    for (int32_t i = 0; i < ne; i++) cnt[key[i] + 1]++;
-    for (int c = 0; c < nkey; c++) cnt[c + 1] += cnt[c];
-    for (int32_t i = 0; i < ne; i++) {
-      const int32_t e = in ? in[i] : i;
-      out[cnt[key[e]]++] = e;
-    }
-  };
-  count_sort(ecol, GW, nullptr, order.data());
+  std::vector<int32_t> order(ne), seg(ne);
+  count_sort(par, ne, GW, ecol.data(), nullptr, [&](int32_t q, int32_t e) { order[q] = e; });
   std::vector<int32_t>().swap(ecol);
-  count_sort(eb, n, order.data(), seg.data());
+  count_sort(par, ne, n, eb.data(), order.data(), [&](int32_t q, int32_t e) { seg[q] = e; });
   // the last pass, by a, carries each element's regions and strength along
   std::vector<int32_t> sa(ne), sb(ne);
   std::vector<double> sv(ne);
-  std::fill(cnt.begin(), cnt.begin() + n + 1, 0);
-  for (int32_t i = 0; i < ne; i++) cnt[ea[i] + 1]++;
-  for (int c = 0; c < n; c++) cnt[c + 1] += cnt[c];
-  for (int32_t i = 0; i < ne; i++) {
-    const int32_t e = seg[i], q = cnt[ea[e]]++;
+  count_sort(par, ne, n, ea.data(), seg.data(), [&](int32_t q, int32_t e) {
     order[q] = e;
     sa[q] = ea[e];
     sb[q] = eb[e];
     sv[q] = ev[e];
-  }
+  });
   std::vector<int32_t>().swap(eb);
   std::vector<int32_t>().swap(ea);
   std::vector<double>().swap(ev);
@@ -1292,52 +1332,64 @@ enum MapForm { kRaw, kCalibrated, kCalibratedHalf };
 // (from 0).  kRaw and kCalibrated write the (2H+1) x (2W+1) grid, the
 // latter calibrated; kCalibratedHalf writes Contours2Ucm's (H+1) x (W+1)
 // output (contours2ucm.cpp:476-486): calibrated point (2r+2, 2c+2) at
-// (r, c) for r < H, c < W, and 0 in the last row and column.  That form
-// keeps three grid rows at a time.
+// (r, c) for r < H, c < W, and 0 in the last row and column, keeping three
+// grid rows at a time.
+//
+// Bands of even rows x0 <= x < x1 run independently: a band owns grid rows
+// x0 .. x1-1 and builds its own copy of the odd row above it, which the
+// band before owns.
 static void write_map(const std::vector<int32_t>& ec, const std::vector<double>& eval, int H, int W, MapForm form,
-                      double* out) {
+                      double* out, const ParFor* par) {
   const int GW = 2 * W + 1, GH = 2 * H + 1;
   const bool half = form == kCalibratedHalf;
-  std::vector<double> ring(half ? 3 * (size_t)GW : 0);
-  auto row_at = [&](int r) { return half ? ring.data() + (size_t)(r % 3) * GW : out + (size_t)r * GW; };
-  Calibrate cal;
-  const size_t ne = ec.size();
-  size_t e = 0;
-  auto fill_row = [&](int r) {
-    double* row = row_at(r);
-    memset(row, 0, sizeof(double) * GW);
-    const int32_t base = r * GW, end = base + GW;
-    for (; e < ne && ec[e] < end; e++)
-      if (eval[e] > 0.0) row[ec[e] - base] = eval[e];
-  };
-  auto calibrate_row = [&](int r) {
-    double* row = row_at(r);
-    for (int y = 0; y < GW; y++) row[y] = cal(row[y]);
-  };
-  for (int x = 0; x < GH; x += 2) {
-    fill_row(x);
-    if (x + 1 < GH) fill_row(x + 1);
-    double* row = row_at(x);
-    const double* below = x + 1 < GH ? row_at(x + 1) : nullptr;
-    const double* above = x >= 1 ? row_at(x - 1) : nullptr;
-    for (int y = 0; y < GW; y += 2) {
-      double m = 0.0;
-      if (below && m < below[y]) m = below[y];
-      if (y + 1 < GW && m < row[y + 1]) m = row[y + 1];
-      if (above && m < above[y]) m = above[y];
-      if (y >= 1 && m < row[y - 1]) m = row[y - 1];
-      row[y] = m;
+  const int nband = par ? std::min(kChunks, H + 1) : 1;
+  auto band_lo = [&](int t) { return 2 * (int)((int64_t)(H + 1) * t / nband); };  // even rows
+  for_chunks(par, nband, [&](int t) {
+    const int x0 = band_lo(t), x1 = band_lo(t + 1);
+    std::vector<double> ring(half ? 3 * (size_t)GW : 0), above0(x0 > 0 ? GW : 0);
+    auto row_at = [&](int r) {
+      if (half) return ring.data() + (size_t)(r % 3) * GW;
+      return r < x0 ? above0.data() : out + (size_t)r * GW;
+    };
+    Calibrate cal;
+    auto fill_row = [&](int r) {
+      double* row = row_at(r);
+      memset(row, 0, sizeof(double) * GW);
+      const int32_t base = r * GW, end = base + GW;
+      for (size_t e = std::lower_bound(ec.begin(), ec.end(), base) - ec.begin(); e < ec.size() && ec[e] < end; e++)
+        if (eval[e] > 0.0) row[ec[e] - base] = eval[e];
+    };
+    auto calibrate_row = [&](int r) {
+      double* row = row_at(r);
+      for (int y = 0; y < GW; y++) row[y] = cal(row[y]);
+    };
+    if (x0 > 0) fill_row(x0 - 1);
+    for (int x = x0; x < x1 && x < GH; x += 2) {
+      fill_row(x);
+      if (x + 1 < GH) fill_row(x + 1);
+      double* row = row_at(x);
+      const double* below = x + 1 < GH ? row_at(x + 1) : nullptr;
+      const double* above = x >= 1 ? row_at(x - 1) : nullptr;
+      for (int y = 0; y < GW; y += 2) {
+        double m = 0.0;
+        if (below && m < below[y]) m = below[y];
+        if (y + 1 < GW && m < row[y + 1]) m = row[y + 1];
+        if (above && m < above[y]) m = above[y];
+        if (y >= 1 && m < row[y - 1]) m = row[y - 1];
+        row[y] = m;
+      }
+      // rows x - 1 and x are final: no later step of this band reads them
+      if (form == kCalibrated) {
+        if (x - 1 > x0) calibrate_row(x - 1);
+        calibrate_row(x);
+      } else if (half && x >= 2) {
+        double* o = out + (size_t)(x / 2 - 1) * (W + 1);
+        for (int c = 0; c < W; c++) o[c] = cal(row[2 * c + 2]);
+        o[W] = 0.0;
+      }
     }
-    // rows x - 1 and x are final: no later step reads them
-    if (form == kCalibrated) {
-      if (x >= 1) calibrate_row(x - 1);
-      calibrate_row(x);
-    } else if (half && x >= 2) {
-      double* o = out + (size_t)(x / 2 - 1) * (W + 1);
-      for (int c = 0; c < W; c++) o[c] = cal(row[2 * c + 2]);
-      o[W] = 0.0;
-    }
-  }
+    if (form == kCalibrated && x1 - 1 < GH && x1 - 1 > x0) calibrate_row(x1 - 1);  // the band's last odd row
+  });
   if (half)
     for (int c = 0; c <= W; c++) out[(size_t)H * (W + 1) + c] = 0.0;
 }
@@ -1345,15 +1397,15 @@ static void write_map(const std::vector<int32_t>& ec, const std::vector<double>&
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm) {
   std::vector<int32_t> ec;
   std::vector<double> ev;
-  merge_impl(lb, part, H, W, ec, ev);
-  write_map(ec, ev, H, W, kRaw, ucm);
+  merge_impl(lb, part, H, W, ec, ev, nullptr);
+  write_map(ec, ev, H, W, kRaw, ucm, nullptr);
 }
 
-void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out) {
+void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out, const ParFor* par) {
   std::vector<int32_t> ec;
   std::vector<double> ev;
-  merge_impl(lb, part, H, W, ec, ev);
-  write_map(ec, ev, H, W, half ? kCalibratedHalf : kCalibrated, out);
+  merge_impl(lb, part, H, W, ec, ev, par);
+  write_map(ec, ev, H, W, half ? kCalibratedHalf : kCalibrated, out, par);
 }
 
 // NormalizeOutput over a whole map

@@ -24,8 +24,10 @@ int edge_orientation(int x1, int y1, int x2, int y2);
 // UcmMeanPb: the (2H+1) x (2W+1) map before calibration
 void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* ucm);
 // the same on float strengths, calibrated (NormalizeOutput): the doubled
-// grid, or with half Contours2Ucm's (H+1) x (W+1) output
-void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out);
+// grid, or with half Contours2Ucm's (H+1) x (W+1) output; with par the
+// setup and the output run on the pool (the merge itself is sequential)
+void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out,
+                 const ParFor* par = nullptr);
 void normalize(double* u, size_t n);
 
 }  // namespace ucm
