@@ -912,15 +912,16 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
 // is the warm start; without one it is seeded noise.
 static void lowdin(const double* G, int n, double* M) {
   // M = G^-1/2 (eigenvalues clamped), so that U M has orthonormal columns
-  std::vector<double> A(G, G + (size_t)n * n), w(n), Z((size_t)n * n);
+  std::vector<double> A(G, G + (size_t)n * n), w(n), Z((size_t)n * n), sq(n);
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) A[i * n + j] = 0.5 * (G[i * n + j] + G[j * n + i]);
   gpb::sym_eig(A.data(), n, w.data(), Z.data());
   const double floor_ = std::max(w[n - 1], 1e-300) * 1e-15;
+  for (int k = 0; k < n; k++) sq[k] = sqrt(std::max(w[k], floor_));
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++) {
       double v = 0;
-      for (int k = 0; k < n; k++) v += Z[i * n + k] * Z[j * n + k] / sqrt(std::max(w[k], floor_));
+      for (int k = 0; k < n; k++) v += Z[i * n + k] * Z[j * n + k] / sq[k];
       M[i * n + j] = v;
     }
 }
