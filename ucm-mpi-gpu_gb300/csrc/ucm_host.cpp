@@ -30,9 +30,8 @@
 
 #include <algorithm>
 #include <deque>
-#include <map>
+#include <functional>
 #include <new>
-#include <queue>
 #include <utility>
 #include <vector>
 
