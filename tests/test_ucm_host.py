@@ -210,3 +210,43 @@ def test_host_stages_reject_sizes_beyond_32_bit_indices():
     bw, i32 = np.zeros(1, np.uint8), np.zeros(4, np.int32)
     assert L.gpb_ucm_fit_contours(bw.ctypes.data, 50000, 50000, 1, 1, 1, i32.ctypes.data, i32.ctypes.data,
                                   i32.ctypes.data, i32.ctypes.data, i32.ctypes.data) == -1
+
+
+def _edge_label_maps():
+    rng = np.random.default_rng(29)
+    yield "1x1", np.zeros((1, 1), np.int32)
+    yield "1x9", np.array([[0, 0, 1, 1, 2, 0, 3, 3, 1]], np.int32)
+    yield "9x1", np.array([[0], [1], [1], [2], [0], [0], [3], [2], [2]], np.int32)
+    yield "one region", np.zeros((6, 7), np.int32)
+    yield "two halves", np.repeat(np.array([[0, 0, 0, 1, 1, 1, 1]], np.int32), 5, axis=0)
+    yield "ids with gaps", (_voronoi(20, 17, 12, rng) * 5).astype(np.int32)
+    yield "checkerboard", (np.indices((8, 8)).sum(0) % 2).astype(np.int32)
+    yield "stripes", np.tile(np.arange(9, dtype=np.int32), (4, 1))
+
+
+@pytest.mark.parametrize("case", [c for c, _ in _edge_label_maps()])
+def test_merge_edge_layouts_against_reference(ref, case):
+    """degenerate shapes and layouts: single pixels, single rows and
+    columns, no boundary at all, unused ids, every pixel its own neighbour's
+    opposite"""
+    import gpb
+    lab = dict(_edge_label_maps())[case]
+    H, W = lab.shape
+    rng = np.random.default_rng(H * 100 + W)
+    for w2 in (rng.random((2 * H + 1, 2 * W + 1)), np.full((2 * H + 1, 2 * W + 1), 0.25)):
+        w2 = np.ascontiguousarray(w2)
+        u = np.zeros_like(w2)
+        ref.ref().ref_ucm_mean_pb(_P(w2), _P(np.ascontiguousarray(lab)), H, W, _P(u))
+        assert np.array_equal(gpb.ucm_mean_pb(w2, lab), u)
+
+
+def test_merge_negative_labels_are_skipped():
+    """pixels with a negative id (the reference indexes region -1 there)
+    take part in no boundary; the library skips them as the oracle does"""
+    import gpb
+    rng = np.random.default_rng(31)
+    lab = _voronoi(24, 30, 40, rng)
+    lab[rng.random(lab.shape) < 0.1] = -1
+    w2 = np.ascontiguousarray(rng.random((49, 61)))
+    u = gpb.ucm_mean_pb(w2, lab)
+    assert np.array_equal(u, uo.mean_pb(w2, lab.astype(np.int64)))
