@@ -250,3 +250,27 @@ def test_merge_negative_labels_are_skipped():
     w2 = np.ascontiguousarray(rng.random((49, 61)))
     u = gpb.ucm_mean_pb(w2, lab)
     assert np.array_equal(u, uo.mean_pb(w2, lab.astype(np.int64)))
+
+
+def _edge_arc_maps():
+    z = lambda h, w: np.zeros((h, w), np.uint8)  # noqa: E731
+    m = z(1, 1); m[0, 0] = 1; yield "pixel", m
+    m = z(1, 12); m[0, 2:10] = 1; yield "row", m
+    m = z(12, 1); m[1:11, 0] = 1; yield "column", m
+    m = z(6, 6); m[2:4, 2:4] = 1; yield "2x2 block", m
+    m = z(7, 7); m[1:6, 1:6] = 1; yield "5x5 block", m
+    m = z(9, 9); m[1, 1:8] = m[7, 1:8] = m[1:8, 1] = m[1:8, 7] = 1; yield "square loop", m
+    m = z(9, 9); m[4, :] = m[:, 4] = 1; yield "plus", m
+    m = z(11, 11); np.fill_diagonal(m, 1); m[np.arange(11), 10 - np.arange(11)] = 1; yield "x", m
+    m = z(10, 14); m[2, 1:13] = m[7, 1:13] = 1; m[2:8, 3] = m[2:8, 10] = 1; m[4, 3:11] = 1; yield "ladder", m
+    yield "all arcs", np.ones((5, 6), np.uint8)
+
+
+@pytest.mark.parametrize("case", [c for c, _ in _edge_arc_maps()])
+def test_fit_edge_maps_against_reference(ref, case):
+    import gpb
+    bw = np.ascontiguousarray(dict(_edge_arc_maps())[case])
+    mine, theirs = gpb.ucm_fit_contours(bw), _ref_fit(ref.ref(), bw)
+    assert mine is not None
+    for a, b in zip(mine, theirs):
+        assert np.array_equal(a, b)
