@@ -61,7 +61,7 @@ def test_library_host_merge_matches_reference(gold, case):
     assert np.abs(uo.normalize(u) - g["ucm2"]).max() <= UCM_TOL
 
 
-@pytest.mark.parametrize("k", [0.05, 0.2, 0.5])
+@pytest.mark.parametrize("k", [-1.0, 0.0, 0.05, 0.2, 0.5, 1.0, 2.0])
 def test_labels_at_scale(gold, k):
     import gpb
     u2 = gold["rand80x64"]["ucm2"]
