@@ -342,6 +342,9 @@ gpb_status gpb_warmnet_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* width
 
 int gpb_device_count(void);
 const char* gpb_status_str(gpb_status s);
+/* The message of the most recent failed call on the context ("" before
+ * any); valid until the next call on the context. */
+const char* gpb_last_error(const gpb_ctx* ctx);
 void gpb_free(void* p);
 
 #ifdef __cplusplus

@@ -300,6 +300,8 @@ extern "C" const char* gpb_status_str(gpb_status s) {
 
 extern "C" void gpb_free(void* p) { free(p); }
 
+extern "C" const char* gpb_last_error(const gpb_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
 extern "C" int gpb_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;

@@ -109,6 +109,8 @@ def _lib():
         L.gpb_device_count.restype = c
         L.gpb_status_str.argtypes = [c]
         L.gpb_status_str.restype = ctypes.c_char_p
+        L.gpb_last_error.argtypes = [vp]
+        L.gpb_last_error.restype = ctypes.c_char_p
         L.gpb_free.argtypes = [vp]
         L.gpb_stitch_device.argtypes = [vp, c, ctypes.c_uint32, ctypes.c_uint32, vp, sz, c, vp, vp]
         L.gpb_stitch_device.restype = c
@@ -155,19 +157,27 @@ def device_count():
     return _lib().gpb_device_count()
 
 
-def _check(st, what, allow_noconv=False):
+def _check(st, what, allow_noconv=False, h=None):
     if st == GPB_OK or (allow_noconv and st == GPB_ERR_NOCONV):
         return
-    raise GpbError(st, what)
+    msg = _lib().gpb_last_error(h).decode() if h else ""
+    raise GpbError(st, "%s [%s]" % (what, msg) if msg else what)
 
 
 class Context:
     """One libgpb context (device buffers, stream, tables)."""
 
+    def _ck(self, st, what, allow_noconv=False):
+        _check(st, what, allow_noconv, self._h)
+
+    def last_error(self):
+        """the message of the most recent failed call on this context"""
+        return _lib().gpb_last_error(self._h).decode() if self._h else ""
+
     def __init__(self, codebook=None, **params):
         self._h = ctypes.c_void_p()
         self.params = default_params(**params)
-        _check(_lib().gpb_create(ctypes.byref(self._h), ctypes.byref(self.params)), "gpb_create")
+        self._ck(_lib().gpb_create(ctypes.byref(self._h), ctypes.byref(self.params)), "gpb_create")
         if codebook is not None:
             self.set_codebook(codebook)
 
@@ -186,10 +196,10 @@ class Context:
         cb = np.ascontiguousarray(codebook, np.float32)
         if cb.ndim != 2 or cb.shape[0] != 13:
             raise ValueError("codebook must be 13 x K")
-        _check(_lib().gpb_set_codebook(self._h, cb.ctypes.data, cb.shape[1]), "gpb_set_codebook")
+        self._ck(_lib().gpb_set_codebook(self._h, cb.ctypes.data, cb.shape[1]), "gpb_set_codebook")
 
     def load_codebook_yml(self, path):
-        _check(_lib().gpb_load_codebook_yml(self._h, path.encode()), "gpb_load_codebook_yml")
+        self._ck(_lib().gpb_load_codebook_yml(self._h, path.encode()), "gpb_load_codebook_yml")
 
     def compute_batch(self, packed_list):
         """packed_list: uint32 H x W arrays (B<<16|G<<8|R).  Returns a list of
@@ -207,7 +217,7 @@ class Context:
             pt[i] = Patch(W, H, a.ctypes.data, W)
             res[i] = Result(nm.ctypes.data, orr.ctypes.data)
         st = _lib().gpb_compute_batch(self._h, pt, n, res)
-        _check(st, "gpb_compute_batch", allow_noconv=True)
+        self._ck(st, "gpb_compute_batch", allow_noconv=True)
         self.last_status = st
         return outs
 
@@ -219,13 +229,13 @@ class Context:
         o = np.ascontiguousarray(offsets, np.uint64)
         st = _lib().gpb_compute_batch_device(self._h, n, w.ctypes.data, h.ctypes.data, o.ctypes.data,
                                              d_packed, d_nmax, d_orient)
-        _check(st, "gpb_compute_batch_device", allow_noconv=True)
+        self._ck(st, "gpb_compute_batch_device", allow_noconv=True)
         self.last_status = st
         return st
 
     def fetch(self, stage, patch, shape, dtype):
         out = np.empty(shape, dtype)
-        _check(_lib().gpb_fetch(self._h, STAGES[stage], patch, out.ctypes.data, out.nbytes), "gpb_fetch")
+        self._ck(_lib().gpb_fetch(self._h, STAGES[stage], patch, out.ctypes.data, out.nbytes), "gpb_fetch")
         return out
 
     def stitch_device(self, mode, width, height, places, d_nmax, d_orient, ramp=0):
@@ -233,13 +243,13 @@ class Context:
         d_orient) from the last batch; places = [(x0, y0, ix, iy, iw, ih)] per
         patch, in batch order."""
         arr = np.ascontiguousarray(np.asarray(places, np.int32).reshape(-1, 6))
-        _check(_lib().gpb_stitch_device(self._h, mode, width, height, arr.ctypes.data, arr.shape[0], ramp,
+        self._ck(_lib().gpb_stitch_device(self._h, mode, width, height, arr.ctypes.data, arr.shape[0], ramp,
                                         d_nmax, d_orient), "gpb_stitch_device")
 
     def superpixel_features(self, patch, d_labels, n_labels, d_out, bin_step=8, with_textons=True):
         """gpb_superpixel_features: n_labels rows of [texton histogram |
         grey histogram | 0 | mean B G R] into the device doubles at d_out."""
-        _check(_lib().gpb_superpixel_features(self._h, patch, d_labels, n_labels, bin_step, int(with_textons), d_out),
+        self._ck(_lib().gpb_superpixel_features(self._h, patch, d_labels, n_labels, bin_step, int(with_textons), d_out),
                "gpb_superpixel_features")
 
     def texton_labels_static(self, width, height, d_packed, d_labels, stream=None):
@@ -247,7 +257,7 @@ class Context:
         of one device-resident packed image into d_labels, with no allocation;
         d_packed, d_labels and stream are raw device pointers / a stream
         handle.  Only enqueues work on the stream."""
-        _check(_lib().gpb_texton_labels_static(self._h, width, height, d_packed, d_labels, stream),
+        self._ck(_lib().gpb_texton_labels_static(self._h, width, height, d_packed, d_labels, stream),
                "gpb_texton_labels_static")
 
     def ucm(self, orient, double_size=True, d_orient=None, shape=None):
@@ -266,7 +276,7 @@ class Context:
             ptr, on_dev = d_orient, 1
         out = np.empty((2 * H + 1, 2 * W + 1) if double_size else (H + 1, W + 1), np.float64)
         info = UcmInfo()
-        _check(_lib().gpb_ucm(self._h, W, H, ptr, on_dev, 1 if double_size else 0, out.ctypes.data,
+        self._ck(_lib().gpb_ucm(self._h, W, H, ptr, on_dev, 1 if double_size else 0, out.ctypes.data,
                               ctypes.byref(info)), "gpb_ucm")
         self.last_ucm_shapes = [(H, W)]
         return out, info.as_dict()
@@ -283,7 +293,7 @@ class Context:
         ptr_in = (ctypes.c_void_p * n)(*[a.ctypes.data for a in arrs])
         ptr_out = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
         infos = (UcmInfo * n)()
-        _check(_lib().gpb_ucm_batch(self._h, n, ws.ctypes.data, hs.ctypes.data, ptr_in, 0, 1 if double_size else 0,
+        self._ck(_lib().gpb_ucm_batch(self._h, n, ws.ctypes.data, hs.ctypes.data, ptr_in, 0, 1 if double_size else 0,
                                     ptr_out, infos), "gpb_ucm_batch")
         self.last_ucm_shapes = [(int(h), int(w)) for h, w in zip(hs, ws)]
         return [(o, infos[i].as_dict()) for i, o in enumerate(outs)]
@@ -294,20 +304,20 @@ class Context:
         shape, dt = {UCM_QUANT: ((H, W), np.uint8), UCM_ARCS: ((H, W), np.uint8), UCM_WSWT: ((H, W), np.float32),
                      UCM_WSWT2: ((2 * H + 1, 2 * W + 1), np.float32), UCM_REGIONS: ((H, W), np.int32)}[what]
         out = np.empty(shape, dt)
-        _check(_lib().gpb_ucm_fetch(self._h, image, what, out.ctypes.data, out.nbytes), "gpb_ucm_fetch")
+        self._ck(_lib().gpb_ucm_fetch(self._h, image, what, out.ctypes.data, out.nbytes), "gpb_ucm_fetch")
         return out
 
     def warmnet_set(self, weights):
         """Switch the learned warm-start correction on (GPB_WARMNET_PARAMS
         float weights) or off (None)."""
         if weights is None:
-            _check(_lib().gpb_warmnet_set(self._h, None, 0), "gpb_warmnet_set")
+            self._ck(_lib().gpb_warmnet_set(self._h, None, 0), "gpb_warmnet_set")
             return
         w = np.ascontiguousarray(weights, np.float32)
-        _check(_lib().gpb_warmnet_set(self._h, w.ctypes.data, w.size), "gpb_warmnet_set")
+        self._ck(_lib().gpb_warmnet_set(self._h, w.ctypes.data, w.size), "gpb_warmnet_set")
 
     def warmnet_capture(self, on=True):
-        _check(_lib().gpb_warmnet_capture(self._h, 1 if on else 0), "gpb_warmnet_capture")
+        self._ck(_lib().gpb_warmnet_capture(self._h, 1 if on else 0), "gpb_warmnet_capture")
 
     def warmnet_grad_device(self, widths, heights, d_xt, d_mpb, d_vt, weights):
         """Mean squared error and gradient of the correction net over patches
@@ -317,14 +327,14 @@ class Context:
         hs = np.ascontiguousarray(heights, np.uint32)
         loss = ctypes.c_double()
         grad = np.empty(WARMNET_PARAMS, np.float32)
-        _check(_lib().gpb_warmnet_grad_device(self._h, len(ws), ws.ctypes.data, hs.ctypes.data, d_xt, d_mpb, d_vt,
+        self._ck(_lib().gpb_warmnet_grad_device(self._h, len(ws), ws.ctypes.data, hs.ctypes.data, d_xt, d_mpb, d_vt,
                                               w.ctypes.data, ctypes.byref(loss), grad.ctypes.data),
                "gpb_warmnet_grad_device")
         return loss.value, grad
 
     def stats(self):
         s = Stats()
-        _check(_lib().gpb_last_stats(self._h, ctypes.byref(s)), "gpb_last_stats")
+        self._ck(_lib().gpb_last_stats(self._h, ctypes.byref(s)), "gpb_last_stats")
         return s.as_dict()
 
 
