@@ -1,6 +1,7 @@
 // host_pool_check.cpp -- built and run by test_host_pool.py: the host pool
 // runs every item once, rethrows the first exception of an item after all
 // items are done, and stays usable afterwards.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <stdexcept>
@@ -41,6 +42,25 @@ int main() {
   std::atomic<int> after{0};
   pool.run(100, [&](int) { after++; });
   fails += after != 100;
+  // copies cut into pieces land exactly once
+  {
+    const size_t piece = 4096;
+    std::vector<size_t> sizes = {0, 1, piece - 1, piece, piece + 1, 5 * piece + 123, 64 * piece};
+    std::vector<std::vector<unsigned char>> src, dst;
+    std::vector<gpb::CopyJob> jobs;
+    unsigned v = 1;
+    for (size_t b : sizes) {
+      src.emplace_back(b);
+      dst.emplace_back(b + 2, 0xAB);  // a guard byte on each side
+      for (auto& c : src.back()) c = (unsigned char)(v = v * 1103515245u + 12345u) >> 3;
+    }
+    for (size_t k = 0; k < sizes.size(); k++) jobs.push_back({dst[k].data() + 1, src[k].data(), sizes[k]});
+    gpb::parallel_copy(pool, jobs, piece);
+    for (size_t k = 0; k < sizes.size(); k++) {
+      fails += dst[k].front() != 0xAB || dst[k].back() != 0xAB;
+      fails += !std::equal(src[k].begin(), src[k].end(), dst[k].begin() + 1);
+    }
+  }
   std::printf("host pool: %d failures\n", fails);
   return fails != 0;
 }

@@ -1254,12 +1254,18 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
       CK(cudaMallocHost(&ctx->h_packed, L.total_pix * sizeof(uint32_t)));
       ctx->c_hpacked = L.total_pix;
     }
+    std::vector<CopyJob> jobs;  // the caller's rows to the staging, on the host pool
     for (size_t i = 0; i < n; i++) {
       const PatchDev& P = L.patches[i];
-      for (int y = 0; y < P.H; y++)
-        memcpy(ctx->h_packed + P.pix + (size_t)y * P.W, host_in[i] + (size_t)y * host_stride[i],
-               (size_t)P.W * sizeof(uint32_t));
+      if (host_stride[i] == (size_t)P.W) {
+        jobs.push_back({ctx->h_packed + P.pix, host_in[i], (size_t)P.N * sizeof(uint32_t)});
+      } else {
+        for (int y = 0; y < P.H; y++)
+          jobs.push_back({ctx->h_packed + P.pix + (size_t)y * P.W, host_in[i] + (size_t)y * host_stride[i],
+                          (size_t)P.W * sizeof(uint32_t)});
+      }
     }
+    parallel_copy(ctx->host_pool(), jobs);
     CK(cudaMemcpyAsync(b.packed, ctx->h_packed, L.total_pix * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   } else {
     for (size_t i = 0; i < n; i++) {
@@ -1348,16 +1354,18 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   }
   CK(cudaEventRecord(ctx->ev[8], s));
   CK(cudaStreamSynchronize(s));
-  if (host_out) {
+  if (host_out) {  // staging to the caller's buffers, on the host pool
+    std::vector<CopyJob> jobs;
     for (size_t i = 0; i < n; i++) {
       const PatchDev& P = L.patches[i];
       gpb_result& r = host_out[i];
       if (!r.nmax) r.nmax = (float*)malloc((size_t)P.N * sizeof(float));
       if (!r.orient) r.orient = (float*)malloc(8 * (size_t)P.N * sizeof(float));
       if (!r.nmax || !r.orient) return GPB_ERR_NOMEM;
-      memcpy(r.nmax, ctx->h_out + P.pix, (size_t)P.N * sizeof(float));
-      memcpy(r.orient, ctx->h_out + L.total_pix + 8 * P.pix, 8 * (size_t)P.N * sizeof(float));
+      jobs.push_back({r.nmax, ctx->h_out + P.pix, (size_t)P.N * sizeof(float)});
+      jobs.push_back({r.orient, ctx->h_out + L.total_pix + 8 * P.pix, 8 * (size_t)P.N * sizeof(float)});
     }
+    parallel_copy(ctx->host_pool(), jobs);
   }
   float ms[9];
   for (int i = 1; i <= 8; i++) cudaEventElapsedTime(&ms[i], ctx->ev[i - 1], ctx->ev[i]);

@@ -7,6 +7,8 @@
 #include <functional>
 #include <mutex>
 #include <stdint.h>
+#include <string.h>
+#include <algorithm>
 #include <thread>
 #include <vector>
 
@@ -92,5 +94,22 @@ class HostPool {
   uint64_t gen_ = 0;
   bool quit_ = false;
 };
+
+// One host copy of `bytes` bytes from src to dst.
+struct CopyJob {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+
+// Runs the copies on the pool, cut into pieces of at most `piece` bytes so
+// that a few large copies spread over the workers too.
+inline void parallel_copy(HostPool& pool, const std::vector<CopyJob>& jobs, size_t piece = (size_t)1 << 20) {
+  std::vector<CopyJob> parts;
+  for (const CopyJob& j : jobs)
+    for (size_t off = 0; off < j.bytes; off += piece)
+      parts.push_back({(char*)j.dst + off, (const char*)j.src + off, std::min(piece, j.bytes - off)});
+  pool.run((int)parts.size(), [&](int i) { memcpy(parts[i].dst, parts[i].src, parts[i].bytes); });
+}
 
 }  // namespace gpb
