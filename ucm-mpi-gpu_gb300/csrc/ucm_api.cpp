@@ -205,19 +205,9 @@ extern "C" gpb_status gpb_ucm_batch(gpb_ctx* ctx, size_t n, const uint32_t* widt
     const ucm::ParFor pool = [&](int k, const std::function<void(int)>& f) { ctx_parallel_for(ctx, k, f); };
     ctx_parallel_for(ctx, ni, [&](int i) {
       const auto ti = std::chrono::steady_clock::now();
-      // one image alone uses the pool inside its contour fitting instead
+      // one image alone uses the pool inside its contour fitting and paint list instead
       ok[i] = ucm::fit_contours(bw.data() + pix[i], H[i], W[i], fit[i], n == 1 ? &pool : nullptr);
-      const ucm::FitResult& f = fit[i];
-      const int ne = (int)f.es.size();
-      ppix[i].reserve(f.px.size() + 2 * ne);
-      pori[i].reserve(f.px.size() + 2 * ne);
-      for (int e = 0; e < ne; e++) {
-        const int a = f.es[e], b = f.ee[e];
-        const uint8_t o = (uint8_t)ucm::edge_orientation(f.vx[a], f.vy[a], f.vx[b], f.vy[b]);
-        for (int k = f.off[e]; k < f.off[e + 1]; k++) ppix[i].push_back(f.px[k]), pori[i].push_back(o);
-        ppix[i].push_back(f.vx[a] * W[i] + f.vy[a]), pori[i].push_back(o);
-        ppix[i].push_back(f.vx[b] * W[i] + f.vy[b]), pori[i].push_back(o);
-      }
+      ucm::paint_list(fit[i], W[i], ppix[i], pori[i], n == 1 ? &pool : nullptr);
       ms_fit_i[i] = ms_since(ti);
     });
     const double ms_fit = ms_since(t1);

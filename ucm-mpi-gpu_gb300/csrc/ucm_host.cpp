@@ -1407,6 +1407,33 @@ void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, 
   write_map(ec, ev, H, W, half ? kCalibratedHalf : kCalibrated, out, par);
 }
 
+// The pixels painted along each edge -- its interior pixels, then its two
+// end points -- each with the edge's orientation bin (contours2ucm.cpp:
+// 331-399).  Edge e's entries start at off[e] + 2e, so bands of edges fill
+// theirs independently.
+void paint_list(const FitResult& f, int W, std::vector<int32_t>& pix, std::vector<uint8_t>& ori, const ParFor* par) {
+  const int ne = (int)f.es.size();
+  const size_t total = (size_t)f.off[ne] + 2 * (size_t)ne;
+  pix.resize(total);
+  ori.resize(total);
+  const int nt = par ? std::min(kChunks, std::max(ne, 1)) : 1;
+  for_chunks(par, nt, [&](int t) {
+    for (int e = (int)((int64_t)ne * t / nt); e < (int)((int64_t)ne * (t + 1) / nt); e++) {
+      const int a = f.es[e], b = f.ee[e];
+      const uint8_t o = (uint8_t)edge_orientation(f.vx[a], f.vy[a], f.vx[b], f.vy[b]);
+      size_t q = (size_t)f.off[e] + 2 * (size_t)e;
+      for (int k = f.off[e]; k < f.off[e + 1]; k++, q++) {
+        pix[q] = f.px[k];
+        ori[q] = o;
+      }
+      pix[q] = f.vx[a] * W + f.vy[a];
+      ori[q++] = o;
+      pix[q] = f.vx[b] * W + f.vy[b];
+      ori[q] = o;
+    }
+  });
+}
+
 // NormalizeOutput over a whole map
 void normalize(double* u, size_t n) {
   Calibrate cal;

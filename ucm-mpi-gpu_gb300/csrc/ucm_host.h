@@ -29,6 +29,10 @@ void mean_pb_merge(const double* lb, const int32_t* part, int H, int W, double* 
 void mean_pb_ucm(const float* lb, const int32_t* part, int H, int W, bool half, double* out,
                  const ParFor* par = nullptr);
 void normalize(double* u, size_t n);
+// the pixels painted along the edges with their orientation bins, edge by
+// edge: interior pixels, then the two end points
+void paint_list(const FitResult& f, int W, std::vector<int32_t>& pix, std::vector<uint8_t>& ori,
+                const ParFor* par = nullptr);
 
 }  // namespace ucm
 }  // namespace gpb
