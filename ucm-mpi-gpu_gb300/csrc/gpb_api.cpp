@@ -1247,7 +1247,6 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   CK(cudaMemcpyAsync(b.tile_begin, L.tile_begin.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(b.tile_count, L.tile_count.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
   // input
-  const uint32_t* d_packed = b.packed;
   if (host_in) {
     if (ctx->c_hpacked < (size_t)L.total_pix) {
       if (ctx->h_packed) cudaFreeHost(ctx->h_packed);
