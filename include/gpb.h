@@ -242,8 +242,12 @@ gpb_status gpb_write_png_minmax(const char* path, const float* data, uint32_t ro
  *           work overlaps on the GPU (different streams or threads) race and
  *           give wrong labels: put them on one stream, or order them with
  *           events.  The kernels read the codebook from the device's constant
- *           tables, which a compute call of a context with another codebook
- *           reloads: let this call's work finish before starting one. */
+ *           tables; a later call of any context that reloads those tables
+ *           (another codebook or compat mode) first waits, on the GPU, for
+ *           this call's kernels.
+ * Reset     the array's address is kept per device for the life of the
+ *           process: do not call this entry point after a cudaDeviceReset
+ *           of that device. */
 gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uint32_t height, const uint32_t* d_packed,
                                     uint32_t* d_labels, void* stream);
 

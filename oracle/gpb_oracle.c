@@ -815,6 +815,42 @@ static double pdot(const double* a, const double* b, size_t n) {
   return s;
 }
 
+/* One classical Gram-Schmidt pass of w against the nv basis vectors
+ * V[0..nv) (each of length n): h[i] (+)= <V_i, w>, then w -= sum_i c_i V_i
+ * with c the pass's own coefficients.  Both sweeps run over the same NCHUNK
+ * fixed row chunks as pdot, so the sums do not depend on the thread count. */
+static void cgs_pass(const double* V, int nv, double* w, size_t n, double* h, int accumulate) {
+  double* part = (double*)malloc(sizeof(double) * NCHUNK * nv);
+  double* c = (double*)malloc(sizeof(double) * nv);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NCHUNK; k++) {
+    const size_t lo = n * k / NCHUNK, hi = n * (k + 1) / NCHUNK;
+    for (int i = 0; i < nv; i++) {
+      const double* vi = V + (size_t)i * n;
+      double s = 0;
+      for (size_t q = lo; q < hi; q++) s += vi[q] * w[q];
+      part[(size_t)k * nv + i] = s;
+    }
+  }
+  for (int i = 0; i < nv; i++) {
+    double s = 0;
+    for (int k = 0; k < NCHUNK; k++) s += part[(size_t)k * nv + i];
+    c[i] = s;
+    h[i] = accumulate ? h[i] + s : s;
+  }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NCHUNK; k++) {
+    const size_t lo = n * k / NCHUNK, hi = n * (k + 1) / NCHUNK;
+    for (int i = 0; i < nv; i++) {
+      const double* vi = V + (size_t)i * n;
+      const double ci = c[i];
+      for (size_t q = lo; q < hi; q++) w[q] -= ci * vi[q];
+    }
+  }
+  free(c);
+  free(part);
+}
+
 /* cyclic Jacobi eigenvalue algorithm for a dense symmetric n x n matrix
  * (Golub & Van Loan, Matrix Computations, sec. 8.5); ascending order */
 static void jacobi_eig(double* A, int n, double* evals, double* V) {
@@ -872,6 +908,10 @@ static void jacobi_eig(double* A, int n, double* evals, double* V) {
   }
 }
 
+#ifndef ORC_KRYLOV_M
+#define ORC_KRYLOV_M(nev) (4 * (nev) + 28)
+#endif
+
 typedef struct {
   const double* Wd;
   const double* dis; /* D^-1/2 */
@@ -919,7 +959,7 @@ int orc_eigs(const double* Wd, int H, int W, int nev, double tol, int maxit, int
   }
   op.dis = dis;
   op.diag = diag;
-  int m = 2 * nev + 16;
+  int m = ORC_KRYLOV_M(nev);
   if ((size_t)m > N) m = (int)N;
   int keep = nev + (m - nev) / 2;
   double* V = (double*)malloc(sizeof(double) * N * (m + 1));
@@ -947,13 +987,13 @@ int orc_eigs(const double* Wd, int H, int W, int nev, double tol, int maxit, int
       double* vj = V + (size_t)j * N;
       lap_apply(&op, vj, w);
       matvecs++;
-      for (int pass = 0; pass < 2; pass++) {
-        for (int i = 0; i <= j; i++) {
-          const double c = pdot(V + (size_t)i * N, w, N);
-          h[i] = (pass == 0) ? c : h[i] + c;
-#pragma omp parallel for schedule(static)
-          for (long q = 0; q < (long)N; q++) w[q] -= c * V[(size_t)i * N + q];
-        }
+      /* full reorthogonalisation: classical Gram-Schmidt, repeated once
+       * when the pass removed more than 1 - 1/sqrt(2) of the norm (the DGKS
+       * test, Daniel, Gragg, Kaufman & Stewart 1976) */
+      {
+        const double n0 = sqrt(pdot(w, w, N));
+        cgs_pass(V, j + 1, w, N, h, 0);
+        if (sqrt(pdot(w, w, N)) < 0.7071067811865476 * n0) cgs_pass(V, j + 1, w, N, h, 1);
       }
       for (int i = 0; i <= j; i++) {
         T[i * m + j] = h[i];

@@ -100,3 +100,30 @@ def test_static_labels_reject_oversize_and_bad_arguments():
         no_cb.texton_labels_static(32, 32, p, p)
     assert e.value.status == gpb.GPB_ERR_ARG
     no_cb.close()
+
+
+def test_static_labels_then_other_codebook_on_another_stream():
+    """A context with another codebook reloads the device's constant tables
+    right after a static call queued behind other work on a side stream: the
+    reload waits for the static call's kernels, which keep their own
+    codebook."""
+    torch = pytest.importorskip("torch")
+    import gpb
+    from gpb import synth
+    a, b, cb_a = _images()
+    cb_b = synth.make_codebook(b, synth.SEED_BASE + 42, n_sample=2048)
+    ca = gpb.Context(cb_a, keep_intermediates=1)
+    cbb = gpb.Context(cb_b)
+    want = _batch_labels(ca, a)
+    pa = _dev(torch, synth.pack_bgr(a))
+    oa = torch.full((a.shape[0] * a.shape[1],), -1, dtype=torch.int32, device="cuda")
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())  # the input copy and the output fill first
+    with torch.cuda.stream(side):
+        torch.cuda._sleep(40_000_000)  # about 20 ms of GPU time ahead of the static kernels
+    ca.texton_labels_static(a.shape[1], a.shape[0], pa.data_ptr(), oa.data_ptr(), side.cuda_stream)
+    cbb.compute_batch([synth.pack_bgr(b)])  # reloads the tables with cb_b
+    torch.cuda.synchronize()
+    assert np.array_equal(oa.cpu().numpy().view(np.uint32), want)
+    ca.close()
+    cbb.close()

@@ -237,6 +237,12 @@ namespace {
 struct ConstBank {
   std::mutex mu;
   uint64_t owner = 0;
+  // Recorded on the caller's stream after gpb_texton_labels_static's kernels,
+  // which read the constant tables outside the context's own stream; a
+  // reload of the tables waits for it first.  Created with the bank's first
+  // context, on its device.
+  cudaEvent_t static_done = nullptr;
+  bool static_pending = false;
 };
 std::mutex g_banks_mu;
 std::map<int, ConstBank*> g_banks;
@@ -258,6 +264,10 @@ static cudaError_t load_tables(gpb_ctx* ctx) {
   // the uploads report through cudaGetLastError: clear an earlier,
   // unrelated non-sticky error first so it is not taken for theirs
   (void)cudaGetLastError();
+  if (bk.static_pending) {  // texton kernels queued on another stream still read the tables
+    cudaStreamWaitEvent(s, bk.static_done, 0);
+    bk.static_pending = false;
+  }
   upload_front(ctx->tab, s);
   upload_cues(ctx->tab, s);
   upload_buildw(ctx->tab, s);
@@ -347,7 +357,9 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
     ctx->token = g_next_token++;
     bool loaded;
     {
-      std::lock_guard<std::mutex> lk(bank_of(ctx->device).mu);
+      ConstBank& bk = bank_of(ctx->device);
+      std::lock_guard<std::mutex> lk(bk.mu);
+      if (!bk.static_done) cudaEventCreateWithFlags(&bk.static_done, cudaEventDisableTiming);
       loaded = load_tables(ctx) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
     }
     if (!loaded) {
@@ -1614,23 +1626,30 @@ extern "C" gpb_status gpb_superpixel_features(gpb_ctx* ctx, size_t patch, const 
 // on the device or the host (no error strings either: the status says it).
 extern "C" gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uint32_t height,
                                                const uint32_t* d_packed, uint32_t* d_labels, void* stream) {
-  if (!ctx || !d_packed || !d_labels || (((uintptr_t)d_packed | (uintptr_t)d_labels) & 3u) || ctx->K == 0 ||
-      width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
-    return GPB_ERR_ARG;
-  const long long N = (long long)width * height;
-  const long long tiles = (long long)((width + 15) / 16) * ((height + 15) / 16);
-  if (N > kStaticMaxPix || tiles > kStaticMaxTiles) return GPB_ERR_TOO_LARGE;
-  if (cudaSetDevice(ctx->device) != cudaSuccess) return GPB_ERR_CUDA;
-  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st;
-  ConstBank& bk = bank_of(ctx->device);
-  std::lock_guard<std::mutex> lk(bk.mu);
-  if (bk.owner != ctx->token) {  // this context's codebook into the constant bank first
-    if (load_tables(ctx) != cudaSuccess || cudaStreamSynchronize(ctx->st) != cudaSuccess) return GPB_ERR_CUDA;
-  }
-  if (launch_texton_static(d_packed, (int)width, (int)height, d_labels, ctx->d_k32_ring, ctx->d_ring_of,
-                           ctx->tab.n_rings, s) != cudaSuccess)
-    return GPB_ERR_CUDA;
-  return GPB_OK;
+  if (!ctx) return GPB_ERR_ARG;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!d_packed || !d_labels || (((uintptr_t)d_packed | (uintptr_t)d_labels) & 3u) || ctx->K == 0 ||
+        width < (uint32_t)kMinSide || height < (uint32_t)kMinSide)
+      return GPB_ERR_ARG;
+    const long long N = (long long)width * height;
+    const long long tiles = (long long)((width + 15) / 16) * ((height + 15) / 16);
+    if (N > kStaticMaxPix || tiles > kStaticMaxTiles) return GPB_ERR_TOO_LARGE;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->st;
+    ConstBank& bk = bank_of(ctx->device);
+    std::lock_guard<std::mutex> lk(bk.mu);
+    if (bk.owner != ctx->token) {  // this context's codebook into the constant bank first
+      CK(load_tables(ctx));
+      CK(cudaStreamSynchronize(ctx->st));
+    }
+    CK(launch_texton_static(d_packed, (int)width, (int)height, d_labels, ctx->d_k32_ring, ctx->d_ring_of,
+                            ctx->tab.n_rings, s));
+    if (bk.static_done) {  // a later reload of the tables waits for these kernels
+      CK(cudaEventRecord(bk.static_done, s));
+      bk.static_pending = true;
+    }
+    return GPB_OK;
+  });
 }
 
 // Accessors for the stages compiled in other translation units.
