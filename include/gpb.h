@@ -37,7 +37,8 @@ typedef enum {
   GPB_ERR_NOCONV = 4,    /* the eigensolver hit its matvec cap                   */
   GPB_ERR_TIMEOUT = 5,   /* a bounded device wait gave up                        */
   GPB_ERR_INTERNAL = 6,  /* an unexpected host exception; the message says more  */
-  GPB_ERR_TOO_LARGE = 7  /* image beyond gpb_texton_labels_static's fixed scratch */
+  GPB_ERR_TOO_LARGE = 7  /* image beyond gpb_texton_labels_static's fixed scratch, or a
+                            batch whose padded vector layout reaches 2^31 entries */
 } gpb_status;
 
 typedef enum {
@@ -72,7 +73,7 @@ typedef struct {
   float warm_tol;        /* residual at which the coarse warm-start solve stops  */
   float eig_gap_frac;    /* block solvers: a patch also needs residual <= this x
                             its smallest gap between wanted eigenvalues (floor
-                            1e-7; 0 disables)                                    */
+                            1e-7; 0 disables; default 0.1)                       */
 } gpb_params;
 
 typedef struct gpb_ctx gpb_ctx;
@@ -105,6 +106,8 @@ typedef struct {
   double spmv_bytes, orth_bytes;
   int eig_fallback;           /* 1: a block solver missed its target and the batch
                                  was solved again by plain Lanczos                 */
+  int graph_replays;          /* launch chains of the last call replayed as CUDA
+                                 graphs (stage chains, filters, Lanczos cycles)    */
 } gpb_stats;
 
 /* intermediates available through gpb_fetch() (keep_intermediates = 1) */

@@ -181,12 +181,98 @@ struct gpb_ctx {
   std::vector<int> pkind;      // 0 spmv, 1 orth
   std::vector<double> pbytes;  // algorithmic bytes of that launch
   size_t pn = 0;
+  // CUDA graphs of fixed launch chains (the stages before and after the
+  // eigensolver, a block solver's filter, a Lanczos restart cycle), keyed by
+  // everything their launches bake in: buffer addresses, sizes, grids
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+  };
+  std::map<std::string, GraphEntry> graphs;
+  bool use_graphs = true;
   std::unique_ptr<HostPool> pool;
   HostPool& host_pool() {
     if (!pool) pool.reset(new HostPool(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))));
     return *pool;
   }
 };
+
+static void drop_graphs(gpb_ctx* ctx) {
+  for (auto& kv : ctx->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  ctx->graphs.clear();
+}
+
+// Runs body() -- stream work on the context's stream, returning the first
+// CUDA error -- as a CUDA graph.  A key seen for the first time runs
+// directly (which also does any one-time set-up of the kernels it launches);
+// the second call with that key captures the work into a graph and launches
+// it; later calls replay the graph.  A capture that fails switches graphs off
+// for the context and runs the work directly.  Off while per-kernel timing
+// is on, and while `allow` is false (a launch in the chain is an autotuner
+// trial).
+template <class F>
+static cudaError_t graph_run(gpb_ctx* ctx, const std::string& key, F&& body, bool allow = true) {
+  cudaStream_t s = ctx->st;
+  if (!ctx->use_graphs || ctx->profile || !allow) return body();
+  auto it = ctx->graphs.find(key);
+  if (it == ctx->graphs.end()) {
+    if (ctx->graphs.size() >= 64) drop_graphs(ctx);
+    ctx->graphs.emplace(key, gpb_ctx::GraphEntry());
+    return body();
+  }
+  gpb_ctx::GraphEntry& g = it->second;
+  if (g.exec) {
+    ctx->launches += g.launches;
+    ctx->stats.graph_replays++;
+    return cudaGraphLaunch(g.exec, s);
+  }
+  const int l0 = ctx->launches;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  const cudaError_t eb = body();
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(s, &graph);
+  cudaGraphExec_t exec = nullptr;
+  if (eb == cudaSuccess && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (eb != cudaSuccess || e != cudaSuccess || !exec) {
+    (void)cudaGetLastError();
+    ctx->use_graphs = false;
+    ctx->launches = l0;
+    return body();
+  }
+  g.exec = exec;
+  g.launches = ctx->launches - l0;
+  return cudaGraphLaunch(exec, s);
+}
+
+// an event record that is also a node of the graph being captured, so stage
+// timings hold for replayed graphs
+static cudaError_t stage_mark(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                             : cudaEventRecord(ev, s);
+}
+
+// a graph key: a tag and the values the captured launches bake in
+template <class... T>
+static std::string gkey(const char* tag, T... v) {
+  std::string k(tag);
+  const long long vals[] = {(long long)v...};
+  for (long long x : vals) k += "," + std::to_string(x);
+  return k;
+}
+
+static int ilog2(long long v) {
+  int r = 0;
+  while (v > 1) {
+    v >>= 1;
+    r++;
+  }
+  return r;
+}
 
 // events around one eigensolver launch (kind 0 = SpMV, 1 = CGS pass)
 static void prof_begin(gpb_ctx* ctx, int kind, double bytes) {
@@ -292,14 +378,14 @@ extern "C" void gpb_default_params(gpb_params* p) {
   p->keep_intermediates = 0;
   p->cheb_degree = 40;
   p->warm_tol = 3e-3f;
-  p->eig_gap_frac = 0.2f;
+  p->eig_gap_frac = 0.1f;
 }
 
 extern "C" const char* gpb_status_str(gpb_status s) {
   switch (s) {
     case GPB_OK: return "ok";
     case GPB_ERR_ARG: return "invalid argument";
-    case GPB_ERR_TOO_LARGE: return "image larger than the entry point's fixed scratch allows";
+    case GPB_ERR_TOO_LARGE: return "image or batch larger than the entry point allows";
     case GPB_ERR_CUDA: return "CUDA error";
     case GPB_ERR_NOMEM: return "out of memory";
     case GPB_ERR_NOCONV: return "eigensolver did not converge";
@@ -351,6 +437,8 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
       ctx->profile = pe && pe[0] == '1';
       const char* tr = getenv("GPB_TRACE");
       ctx->trace = tr && tr[0] == '1';
+      const char* ng = getenv("GPB_NO_GRAPHS");  // launch every chain directly
+      ctx->use_graphs = !(ng && ng[0] == '1');
     }
     build_tables(ctx->tab, q.compat);
     cudaStream_t s = ctx->st;
@@ -415,6 +503,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
   cudaFree(ctx->d_wn_scale);
   cudaFree(ctx->d_wn_x0);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
+  drop_graphs(ctx);
   {
     ConstBank& bk = bank_of(ctx->device);
     std::lock_guard<std::mutex> lk(bk.mu);
@@ -685,6 +774,7 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
   const int np = (int)L.patches.size(), nt = (int)L.tiles.size();
   const int m = q.krylov_dim, keep = q.krylov_keep, nev = q.nvec;
   EigArgs a;
+  memset(&a, 0, sizeof(a));  // its bytes key the restart cycle's graph
   a.patches = b.patches;
   a.tiles = b.tiles;
   a.tile_begin = b.tile_begin;
@@ -727,24 +817,35 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
     long long active_px = 0;
     for (int i = 0; i < np; i++)
       if (active[i]) active_px += L.patches[i].N;
-    for (int j = k; j < m; j++) {
-      const bool from_v = (j == k && !first);
-      // algorithmic bytes per pixel: SpMV reads 40 upper coefficients, the
-      // diagonal and x, writes v_j and w, and reads j basis vectors for the
-      // dots; a CGS pass reads w and j+1 basis vectors and writes w
-      const double npx = (double)active_px;
-      prof_begin(ctx, 0, npx * 4.0 * (kUpper + 1 + 1 + 2 + j));
-      CK(ks_launch_spmv(a, nt, j, from_v ? Vc + (long long)k * L.lvec : cur, from_v ? 0 : 1, nxt, s));
-      prof_end(ctx);
-      prof_begin(ctx, 1, npx * 4.0 * (j + 1 + 2));
-      CK(ks_launch_orth(a, nt, j, 1, nxt, s));
-      prof_end(ctx);
-      prof_begin(ctx, 1, npx * 4.0 * (j + 1 + 2));
-      CK(ks_launch_orth(a, nt, j, 2, nxt, s));
-      prof_end(ctx);
-      ctx->launches += 3;
-      std::swap(cur, nxt);
-    }
+    // one restart cycle: Lanczos steps k .. m-1, three launches each
+    auto cycle = [&]() -> cudaError_t {
+      float* c = cur;
+      float* nx = nxt;
+      for (int j = k; j < m; j++) {
+        const bool from_v = (j == k && !first);
+        // algorithmic bytes per pixel: SpMV reads 40 upper coefficients, the
+        // diagonal and x, writes v_j and w, and reads j basis vectors for the
+        // dots; a CGS pass reads w and j+1 basis vectors and writes w
+        const double npx = (double)active_px;
+        cudaError_t e;
+        prof_begin(ctx, 0, npx * 4.0 * (kUpper + 1 + 1 + 2 + j));
+        if ((e = ks_launch_spmv(a, nt, j, from_v ? Vc + (long long)k * L.lvec : c, from_v ? 0 : 1, nx, s)) !=
+            cudaSuccess)
+          return e;
+        prof_end(ctx);
+        prof_begin(ctx, 1, npx * 4.0 * (j + 1 + 2));
+        if ((e = ks_launch_orth(a, nt, j, 1, nx, s)) != cudaSuccess) return e;
+        prof_end(ctx);
+        prof_begin(ctx, 1, npx * 4.0 * (j + 1 + 2));
+        if ((e = ks_launch_orth(a, nt, j, 2, nx, s)) != cudaSuccess) return e;
+        prof_end(ctx);
+        ctx->launches += 3;
+        std::swap(c, nx);
+      }
+      return cudaSuccess;
+    };
+    CK(graph_run(ctx, gkey("lanczos", k, first, m, nt, cur, nxt) + std::string((const char*)&a, sizeof(a)), cycle));
+    if ((m - k) % 2) std::swap(cur, nxt);
     CK(cudaMemcpyAsync(T.data(), b.T, T.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(beta2.data(), b.beta2, np * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -897,6 +998,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   // started and every patch's vectors stay in X, converged or not
   const int deg = std::min((std::max(3, q.cheb_degree) + 2) / 3 * 3, kMaxCheb / 3 * 3);
   BlkArgs a;
+  memset(&a, 0, sizeof(a));  // its bytes key the filter's graph
   a.patches = lv.patches;
   a.tiles = lv.tiles;
   a.tile_begin = lv.tile_begin;
@@ -1126,17 +1228,26 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
       if (active[i]) apx += L.patches[i].N;
     float* buf[3] = {X, Y, Z};
     int cur = 0;
-    for (int k = 0; k < deg; k++) {
-      const int nxt = (cur + 1) % 3, prv = (cur + 2) % 3;
-      // algorithmic bytes per pixel: the stencil row's coefficients, the
-      // 32-wide rows of Y (and of the previous iterate after the first
-      // step), the output row
-      prof_begin(ctx, 0, (double)apx * (4.0 * (lv.coarse ? kCN : kStencilN) + 4.0 * kBlk * (k ? 3 : 2)));
-      CK(cf_launch_step(a, work_blk, nwb, buf[cur], buf[prv], buf[nxt], k, s));
-      prof_end(ctx);
-      cur = nxt;
-    }
-    ctx->launches += deg;
+    auto filter = [&]() -> cudaError_t {
+      int c = 0;
+      for (int k = 0; k < deg; k++) {
+        const int nxt = (c + 1) % 3, prv = (c + 2) % 3;
+        // algorithmic bytes per pixel: the stencil row's coefficients, the
+        // 32-wide rows of Y (and of the previous iterate after the first
+        // step), the output row
+        prof_begin(ctx, 0, (double)apx * (4.0 * (lv.coarse ? kCN : kStencilN) + 4.0 * kBlk * (k ? 3 : 2)));
+        const cudaError_t e = cf_launch_step(a, work_blk, nwb, buf[c], buf[prv], buf[nxt], k, s);
+        if (e != cudaSuccess) return e;
+        prof_end(ctx);
+        c = nxt;
+      }
+      ctx->launches += deg;
+      return cudaSuccess;
+    };
+    CK(graph_run(ctx,
+                 gkey("filter", deg, nwb, work_blk, X, Y, Z) + std::string((const char*)&a, sizeof(a)),
+                 filter));
+    cur = deg % 3;
     if (buf[cur] != X) {
       ctx->last_error = "block filter rotation out of step";
       return GPB_ERR_INTERNAL;
@@ -1239,6 +1350,11 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   ctx->launches = 0;
   memset(&ctx->stats, 0, sizeof(ctx->stats));
   Layout L = make_layout(n, ws, hs);
+  // the eigensolver kernels index the vector layout with 32-bit offsets
+  if (L.lvec >= (1LL << 31)) {
+    ctx->last_error = "batch too large: its padded vector layout exceeds 2^31 entries; split it";
+    return GPB_ERR_TOO_LARGE;
+  }
   std::string key;
   for (size_t i = 0; i < n; i++) key += std::to_string(ws[i]) + "x" + std::to_string(hs[i]) + ",";
   const bool changed = key != ctx->layout_key;
@@ -1286,34 +1402,52 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     }
   }
   CK(cudaEventRecord(ctx->ev[1], s));
-  // (a) textons
-  CK(launch_convert(b.packed, L.total_pix, b.grey, b.lab4, s));
-  CK(cudaMemsetAsync(b.repair_count, 0, sizeof(int), s));
+  // (a)-(c): textons, local cues, NMS, buildW and the operator rows, one
+  // fixed chain per batch layout
   const int repair_cap = (int)(b.c_repair / 2);
-  CK(launch_texton(b.patches, b.work_tex, (int)L.work_tex.size(), b.grey, b.lab4, b.repair, b.repair_count,
-                   repair_cap, s));
-  CK(launch_texton_repair(b.patches, b.grey, b.lab4, b.repair, b.repair_count, repair_cap, ctx->d_k32_ring,
-                          ctx->d_ring_of, ctx->tab.n_rings, s));
-  CK(cudaEventRecord(ctx->ev[2], s));
-  // (b) local cues + NMS
-  CK(launch_maxlabel(b.patches, (int)np, b.lab4, b.nbins, s));
-  CK(launch_cues(b.patches, b.work_cue, (int)L.work_cue.size(), b.lab4, b.nbins, b.mpbo, b.go,
-                 ctx->prm.keep_intermediates ? b.raw : nullptr,
-                 ctx->prm.keep_intermediates >= 2 ? b.counts : nullptr, s));
-  CK(cudaEventRecord(ctx->ev[3], s));
-  CK(launch_nms(b.patches, b.work16, (int)L.work16.size(), b.mpbo, b.mpb, s));
-  CK(cudaEventRecord(ctx->ev[4], s));
-  // (c) buildW
-  CK(launch_buildw(b.patches, b.work16, (int)L.work16.size(), b.mpb, ctx->d_ic, b.wup, b.deg, L.lvec, s));
-  CK(launch_scale(b.patches, b.work16, (int)L.work16.size(), b.wup, b.deg, b.aup, b.adiag, b.dis, L.lvec,
-                  ctx->prm.keep_intermediates ? b.wfull : nullptr, s));
-  if (ctx->prm.eig_mode != GPB_EIG_LANCZOS) {
-    CK(cf_launch_full(b.patches, b.work16, (int)L.work16.size(), b.aup, b.adiag, L.lvec, b.afull, s));
-    CK(cudaMemsetAsync(b.berr, 0, sizeof(int), s));
-    ctx->launches++;
-  }
-  CK(cudaEventRecord(ctx->ev[5], s));
-  ctx->launches += 10;
+  const bool blockm = ctx->prm.eig_mode != GPB_EIG_LANCZOS;
+  auto pre_chain = [&]() -> cudaError_t {
+    cudaError_t e;
+#define GK(x)                               \
+  do {                                      \
+    if ((e = (x)) != cudaSuccess) return e; \
+  } while (0)
+    // (a) textons
+    GK(launch_convert(b.packed, L.total_pix, b.grey, b.lab4, s));
+    GK(cudaMemsetAsync(b.repair_count, 0, sizeof(int), s));
+    GK(launch_texton(b.patches, b.work_tex, (int)L.work_tex.size(), b.grey, b.lab4, b.repair, b.repair_count,
+                     repair_cap, s));
+    GK(launch_texton_repair(b.patches, b.grey, b.lab4, b.repair, b.repair_count, repair_cap, ctx->d_k32_ring,
+                            ctx->d_ring_of, ctx->tab.n_rings, s));
+    GK(stage_mark(ctx->ev[2], s));
+    // (b) local cues + NMS
+    GK(launch_maxlabel(b.patches, (int)np, b.lab4, b.nbins, s));
+    GK(launch_cues(b.patches, b.work_cue, (int)L.work_cue.size(), b.lab4, b.nbins, b.mpbo, b.go,
+                   ctx->prm.keep_intermediates ? b.raw : nullptr,
+                   ctx->prm.keep_intermediates >= 2 ? b.counts : nullptr, s));
+    GK(stage_mark(ctx->ev[3], s));
+    GK(launch_nms(b.patches, b.work16, (int)L.work16.size(), b.mpbo, b.mpb, s));
+    GK(stage_mark(ctx->ev[4], s));
+    // (c) buildW
+    GK(launch_buildw(b.patches, b.work16, (int)L.work16.size(), b.mpb, ctx->d_ic, b.wup, b.deg, L.lvec, s));
+    GK(launch_scale(b.patches, b.work16, (int)L.work16.size(), b.wup, b.deg, b.aup, b.adiag, b.dis, L.lvec,
+                    ctx->prm.keep_intermediates ? b.wfull : nullptr, s));
+    if (blockm) {
+      GK(cf_launch_full(b.patches, b.work16, (int)L.work16.size(), b.aup, b.adiag, L.lvec, b.afull, s));
+      GK(cudaMemsetAsync(b.berr, 0, sizeof(int), s));
+      ctx->launches++;
+    }
+    GK(stage_mark(ctx->ev[5], s));
+    ctx->launches += 10;
+    return cudaSuccess;
+  };
+  CK(graph_run(ctx,
+               gkey("pre", L.total_pix, L.lvec, np, L.work_tex.size(), L.work_cue.size(), L.work16.size(),
+                    repair_cap, ctx->tab.n_rings, blockm, ctx->prm.keep_intermediates) +
+                   gkey("", b.packed, b.grey, b.lab4, b.repair, b.repair_count, b.patches, b.work_tex, b.work_cue,
+                        b.work16, b.nbins, b.mpbo, b.go, b.raw, b.counts, b.mpb, b.wup, b.deg, b.aup, b.adiag,
+                        b.dis, b.wfull, b.afull, b.berr, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of),
+               pre_chain));
   // (d) eigensolver
   gpb_status es;
   if (warm) {
@@ -1343,27 +1477,42 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     }
   }
   CK(cudaEventRecord(ctx->ev[6], s));
-  // (e) sPb + gPb
+  // (e) sPb + gPb, and the results to the pinned staging
   float* o_nmax = dev_nmax ? dev_nmax : b.nmax;
   float* o_orient = dev_orient ? dev_orient : b.orient;
-  CK(launch_minmax(b.patches, (int)np, b.evec, L.lvec, b.dis, ctx->prm.nvec, b.mm, s));
-  CK(launch_spb(b.patches, b.work16, (int)L.work16.size(), b.evec, L.lvec, b.dis, b.evals, b.mm, ctx->prm.nvec,
-                b.go, b.mpb, ctx->prm.compat, ctx->prm.keep_intermediates ? b.spb : nullptr,
-                ctx->prm.keep_intermediates ? b.gpbo : nullptr, o_nmax, o_orient, s));
-  ctx->launches += 2;
-  CK(cudaEventRecord(ctx->ev[7], s));
   if (host_out) {
     const size_t need = 9 * (size_t)L.total_pix;
     if (ctx->c_hout < need) {
       if (ctx->h_out) cudaFreeHost(ctx->h_out);
+      ctx->h_out = nullptr;
+      ctx->c_hout = 0;
       CK(cudaMallocHost(&ctx->h_out, need * sizeof(float)));
       ctx->c_hout = need;
     }
-    CK(cudaMemcpyAsync(ctx->h_out, o_nmax, L.total_pix * sizeof(float), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(ctx->h_out + L.total_pix, o_orient, 8 * L.total_pix * sizeof(float),
-                       cudaMemcpyDeviceToHost, s));
   }
-  CK(cudaEventRecord(ctx->ev[8], s));
+  auto post_chain = [&]() -> cudaError_t {
+    cudaError_t e;
+    GK(launch_minmax(b.patches, (int)np, b.evec, L.lvec, b.dis, ctx->prm.nvec, b.mm, s));
+    GK(launch_spb(b.patches, b.work16, (int)L.work16.size(), b.evec, L.lvec, b.dis, b.evals, b.mm, ctx->prm.nvec,
+                  b.go, b.mpb, ctx->prm.compat, ctx->prm.keep_intermediates ? b.spb : nullptr,
+                  ctx->prm.keep_intermediates ? b.gpbo : nullptr, o_nmax, o_orient, s));
+    ctx->launches += 2;
+    GK(stage_mark(ctx->ev[7], s));
+    if (host_out) {
+      GK(cudaMemcpyAsync(ctx->h_out, o_nmax, L.total_pix * sizeof(float), cudaMemcpyDeviceToHost, s));
+      GK(cudaMemcpyAsync(ctx->h_out + L.total_pix, o_orient, 8 * L.total_pix * sizeof(float),
+                         cudaMemcpyDeviceToHost, s));
+    }
+    GK(stage_mark(ctx->ev[8], s));
+    return cudaSuccess;
+#undef GK
+  };
+  CK(graph_run(ctx,
+               gkey("post", L.total_pix, L.lvec, np, L.work16.size(), ctx->prm.nvec, ctx->prm.compat,
+                    ctx->prm.keep_intermediates, host_out != nullptr) +
+                   gkey("", b.patches, b.evec, b.dis, b.mm, b.work16, b.evals, b.go, b.mpb, b.spb, b.gpbo, o_nmax,
+                        o_orient, ctx->h_out),
+               post_chain));
   CK(cudaStreamSynchronize(s));
   if (host_out) {  // staging to the caller's buffers, on the host pool
     std::vector<CopyJob> jobs;

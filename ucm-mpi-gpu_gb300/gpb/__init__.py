@@ -70,7 +70,8 @@ class Stats(ctypes.Structure):
         ("max_residual", ctypes.c_float), ("texton_repaired", ctypes.c_long),
         ("gpu_launches", ctypes.c_int), ("spmv_ms", ctypes.c_double), ("orth_ms", ctypes.c_double),
         ("spmv_launches", ctypes.c_long), ("orth_launches", ctypes.c_long),
-        ("spmv_bytes", ctypes.c_double), ("orth_bytes", ctypes.c_double), ("eig_fallback", ctypes.c_int)]
+        ("spmv_bytes", ctypes.c_double), ("orth_bytes", ctypes.c_double), ("eig_fallback", ctypes.c_int),
+        ("graph_replays", ctypes.c_int)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
