@@ -148,15 +148,99 @@ def ucm_case():
 def ncu_case(eig="warm"):
     """One batch of the workload, nothing else: the command that ncu captures
     (a few launches of one kernel out of it).  eig="block" skips the coarse
-    level, so the first block-step launches are fine-level ones."""
+    level, so the first block-step launches are fine-level ones; eig="lanczos"
+    runs the plain cold-start path."""
     import torch
     import gpb
     _, cb, _, patches = make_workload()
-    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM if eig == "warm" else gpb.EIG_BLOCK)
+    mode = {"warm": gpb.EIG_WARM, "block": gpb.EIG_BLOCK, "lanczos": gpb.EIG_LANCZOS}[eig]
+    ctx = gpb.Context(cb, eig_mode=mode)
     ctx.compute_batch(patches)
     torch.cuda.synchronize()
     print(json.dumps({"ncu_case": "done", "gpu_launches": ctx.stats()["gpu_launches"]}))
     ctx.close()
+
+
+def scale_config(name, args):
+    """The uneven (4096^2, 64 rectangles of 200-700 px) or the at-scale
+    (8192^2, 256 x 522^2 with a 5-px halo) workload: one warm batch untimed,
+    then timed batches through the host API (host patches in, host planes
+    out, wall clock); the FP64-checked residual bound from the library's
+    stats and the gPb max error of two sampled patches against the oracle;
+    the plain cold-start Lanczos path on a sample of the patches, per pixel."""
+    import torch
+    import gpb
+    from gpb import synth
+    t0 = time.time()
+    if name == "config3":
+        img, cb, boxes = synth.image_4096_uneven()
+        crops = [np.ascontiguousarray(img[y0:y0 + h, x0:x0 + w]) for (y0, x0, h, w) in boxes]
+        out_px = sum(h * w for (_, _, h, w) in boxes)
+        desc = "4096x4096 Voronoi(4096 cells, sigma 6, 40 lines) -> 64 rectangles, sides U[200,700], one batch"
+        sample = (int(np.argsort([h * w for (_, _, h, w) in boxes])[len(boxes) // 2]), 0)
+    else:
+        img, cb = synth.image_8192()
+        boxes = synth.grid_patches(8192, 8192, 16, 16, 5)
+        crops = [np.ascontiguousarray(img[y0:y0 + h, x0:x0 + w]) for (y0, x0, h, w, *_r) in boxes]
+        out_px = 8192 * 8192
+        desc = "8192x8192 Voronoi(16384 cells, sigma 8, 200 lines) -> 256 x 512^2 patches + 5-px halo, one batch"
+        sample = (37, 200)
+    gen_s = time.time() - t0
+    packed = [synth.pack_bgr(c) for c in crops]
+    in_px = sum(c.shape[0] * c.shape[1] for c in crops)
+
+    def timed(ctx):
+        ctx.compute_batch(packed)  # layout, buffers, autotuning, graphs
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.scale_steps):
+            t1 = time.perf_counter()
+            outs = ctx.compute_batch(packed)
+            ts.append(time.perf_counter() - t1)
+        return float(np.mean(ts)), outs
+
+    ctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
+    sec, outs = timed(ctx)
+    st = ctx.stats()
+    tuning = ctx.tuning_report()
+    ctx.close()
+    errs = {}
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    for i in sample:
+        ref = po.globalpb(crops[i], cb)
+        h, w = crops[i].shape[:2]
+        errs[str(i)] = {"gpb": float(np.abs(outs[i][1].reshape(8, h, w) - ref["gpb_o"]).max()),
+                        "nmax": float(np.abs(outs[i][0] - ref["nmax"]).max()), "shape": [h, w]}
+    out = {"workload": desc, "mpix_s": out_px / sec / 1e6, "s_per_batch": sec, "steps": args.scale_steps,
+           "timing": "wall clock of gpb_compute_batch, host patches in and host planes out",
+           "stages_ms": {kk: st[kk] for kk in ("ms_texton", "ms_cues", "ms_nms", "ms_buildw", "ms_eig", "ms_spb")},
+           "max_residual": st["max_residual"], "matvecs_max": st["matvecs_max"], "eig_fallback": st["eig_fallback"],
+           "graph_replays": st["graph_replays"], "oracle_error": errs, "image_s": gen_s,
+           "tuning": {k: v[0] for k, v in tuning.items()}}
+    if name == "config3":
+        # the same batch with every tunable kernel at its default variant
+        os.environ["GPB_NO_TUNE"] = "1"
+        nt = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
+        os.environ.pop("GPB_NO_TUNE")
+        sec_nt, _ = timed(nt)
+        nt.close()
+        out["untuned"] = {"mpix_s": out_px / sec_nt / 1e6, "s_per_batch": sec_nt}
+    # plain cold-start Lanczos on every k-th patch, Mpix/s of their own share
+    k = max(1, len(crops) // args.scale_plain_patches)
+    pick = list(range(0, len(crops), k))[:args.scale_plain_patches]
+    pl = gpb.Context(cb, eig_mode=gpb.EIG_LANCZOS)
+    pl.compute_batch([packed[i] for i in pick[:1]])
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    pl.compute_batch([packed[i] for i in pick])
+    pdt = time.perf_counter() - t1
+    ppx = sum(crops[i].shape[0] * crops[i].shape[1] for i in pick) * (out_px / in_px)
+    pl.close()
+    out["plain"] = {"mpix_s": ppx / pdt / 1e6, "patches": len(pick), "s": pdt,
+                    "note": "plain cold-start Lanczos on every %d-th patch, Mpix/s of their non-halo share" % k}
+    out["speedup_vs_plain"] = out["mpix_s"] / out["plain"]["mpix_s"]
+    return out
 
 
 def traffic_per_launch(alg_bytes_per_launch):
@@ -334,6 +418,9 @@ def run_gpu(args):
         }
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(img, cb, boxes, seconds=args.cpu_seconds)
+        if not args.no_scale:
+            for name in ("config3", "config5"):
+                out[name] = scale_config(name, args)
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -351,11 +438,14 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-ucm", action="store_true")
+    ap.add_argument("--no-scale", action="store_true", help="skip the 4096^2 uneven and 8192^2 workloads")
+    ap.add_argument("--scale-steps", type=int, default=2)
+    ap.add_argument("--scale-plain-patches", type=int, default=8)
     ap.add_argument("--ucm-case", action="store_true", help="one batch and one OWT-UCM call only (for ncu)")
     ap.add_argument("--ucm-steps", type=int, default=3)
     ap.add_argument("--ucm-save", default=None, help="write the UCM input planes (.npy) to this path and the map beside it")
     ap.add_argument("--ncu-case", action="store_true", help="one batch only (for ncu captures)")
-    ap.add_argument("--ncu-eig", default="warm", choices=["warm", "block"])
+    ap.add_argument("--ncu-eig", default="warm", choices=["warm", "block", "lanczos"])
     args = ap.parse_args()
     if args.ucm_case:
         ucm_case()

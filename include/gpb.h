@@ -164,6 +164,16 @@ gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst, size_t ds
 
 gpb_status gpb_last_stats(gpb_ctx* ctx, gpb_stats* st);
 
+/* The context's autotuner: for each shape bucket of a tunable kernel (the
+ * texton tile's thread count, the block step's X staging and tile queue),
+ * "key=chosen variant (median ms of each variant); ...", -1 while a bucket
+ * is still being tried.  Every variant gives identical results; the first
+ * launches of a bucket try them on real work.  GPB_NO_TUNE=1 in the
+ * environment at gpb_create keeps the default variants.  Writes at most n
+ * bytes including the terminating 0; returns the report's full length.  No
+ * counterpart in the reference. */
+size_t gpb_tuning_report(gpb_ctx* ctx, char* buf, size_t n);
+
 /* Stitching the patches of the last compute call into whole-image planes on
  * the device; replaces Pieces2Gpb (src/utilities.cpp:180-213). */
 typedef enum {

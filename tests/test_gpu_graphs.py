@@ -53,3 +53,29 @@ def test_graph_replays_match_direct_launches(mode):
     for (nm_a, or_a), (nm_b, or_b) in zip(want_sub, got):
         assert np.abs(nm_a - nm_b).max() < 1e-6 and np.abs(or_a - or_b).max() < 1e-6
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_autotuner_settles_and_keeps_results(mode):
+    """The autotuner tries every texton and block-step variant on real work,
+    settles on one per shape bucket, and the results equal the untuned
+    default variants bit for bit on every call."""
+    import gpb
+    cb, patches = _batch()
+    ref = _env_context(cb, mode, "GPB_NO_TUNE")
+    want = ref.compute_batch(patches)
+    assert ref.tuning_report() == {}
+    ref.close()
+    ctx = gpb.Context(cb, eig_mode=mode)
+    for call in range(4):  # texton has 3 variants, one trial per call
+        got = ctx.compute_batch(patches)
+        for (nm_a, or_a), (nm_b, or_b) in zip(want, got):
+            assert np.array_equal(nm_a, nm_b) and np.array_equal(or_a, or_b), call
+    rep = ctx.tuning_report()
+    tex = [k for k in rep if k.startswith("texton/")]
+    steps = [k for k in rep if k.startswith("step/")]
+    assert tex and steps, rep
+    for k in tex:
+        assert rep[k][0] in (0, 1, 2) and len(rep[k][1]) == 3 and min(rep[k][1]) > 0, rep[k]
+    assert any(rep[k][0] >= 0 for k in steps), rep
+    ctx.close()

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/gpb.h"
+#include "autotune.h"
 #include "gpb_internal.h"
 #include "host_pool.h"
 #include "k_block.h"
@@ -190,6 +191,8 @@ struct gpb_ctx {
   };
   std::map<std::string, GraphEntry> graphs;
   bool use_graphs = true;
+  // kernel variants chosen per shape bucket (autotune.h)
+  Autotuner tuner;
   std::unique_ptr<HostPool> pool;
   HostPool& host_pool() {
     if (!pool) pool.reset(new HostPool(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))));
@@ -439,6 +442,8 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
       ctx->trace = tr && tr[0] == '1';
       const char* ng = getenv("GPB_NO_GRAPHS");  // launch every chain directly
       ctx->use_graphs = !(ng && ng[0] == '1');
+      const char* nt = getenv("GPB_NO_TUNE");  // the default variant of every tunable kernel
+      ctx->tuner.enabled = !(nt && nt[0] == '1');
     }
     build_tables(ctx->tab, q.compat);
     cudaStream_t s = ctx->st;
@@ -713,7 +718,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     for (int i = 0; i < 4; i++) es.push_back(grow(b.blk[i], b.c_blk[i], (size_t)kBlk * V));
     es.push_back(grow(b.afull, b.c_afull, (size_t)kFullNC * V));
     es.push_back(grow(b.work_act, b.c_wact, L.work_blk.size()));
-    es.push_back(grow(b.berr, b.c_berr, 1));
+    es.push_back(grow(b.berr, b.c_berr, 4));  // error word, spare, block-step queue [2]
     es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
     es.push_back(grow(b.bgram2, b.c_bgram2, np * kBlk * kBlk));
@@ -1007,6 +1012,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   a.a_diag = nullptr;
   a.afull = lv.afull;
   a.err = b.berr;
+  a.queue = b.berr + 2;
   a.coarse = lv.coarse;
   a.lvec = L.lvec;
   a.coef = b.bcoef;
@@ -1018,6 +1024,15 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
   a.mat = b.bmat;
   a.theta = b.btheta;
   const size_t BB = (size_t)kBlk * kBlk;
+  // block-step variant per level and tile-count bucket
+  auto step_key = [&](int nw) {
+    return std::string(lv.coarse ? "step/coarse" : "step/fine") + "/tiles2^" + std::to_string(ilog2(nw));
+  };
+  auto step_variant = [&](int nw) {
+    bool trial = false;
+    return ctx->tuner.decided(step_key(nw)) ? ctx->tuner.pick(step_key(nw), kStepVariants, 3, kStepDefault, &trial)
+                                            : kStepDefault;
+  };
   std::vector<int> active(np, 1), done(np, 0);
   // G, M, G2 (32 x 32 per patch), theta, res and the filter coefficients
   // live in one pinned block, so their copies are direct DMA
@@ -1081,6 +1096,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     CK(cf_launch_gram(a, nt, F, F, b.bgram, s));
     CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    ctx->tuner.collect();
     ctx->host_pool().run(np, [&](int i) {
       if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
     });
@@ -1090,7 +1106,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
     CK(upload_unit());
-    CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s, comp));
+    CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s, comp, step_variant(nwb)));
     CK(cf_launch_gram(a, nt, F, F, b.bgram2, s));
     CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
     CK(cudaMemcpyAsync(G2.data(), b.bgram2, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1228,6 +1244,8 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
       if (active[i]) apx += L.patches[i].N;
     float* buf[3] = {X, Y, Z};
     int cur = 0;
+    const bool decided = ctx->tuner.decided(step_key(nwb));
+    const int chosen = step_variant(nwb);
     auto filter = [&]() -> cudaError_t {
       int c = 0;
       for (int k = 0; k < deg; k++) {
@@ -1236,7 +1254,11 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
         // 32-wide rows of Y (and of the previous iterate after the first
         // step), the output row
         prof_begin(ctx, 0, (double)apx * (4.0 * (lv.coarse ? kCN : kStencilN) + 4.0 * kBlk * (k ? 3 : 2)));
-        const cudaError_t e = cf_launch_step(a, work_blk, nwb, buf[c], buf[prv], buf[nxt], k, s);
+        bool trial = false;
+        const int v = decided ? chosen : ctx->tuner.pick(step_key(nwb), kStepVariants, 3, chosen, &trial);
+        if (trial) ctx->tuner.begin(step_key(nwb), v, s);
+        const cudaError_t e = cf_launch_step(a, work_blk, nwb, buf[c], buf[prv], buf[nxt], k, s, false, v);
+        if (trial) ctx->tuner.end(s);
         if (e != cudaSuccess) return e;
         prof_end(ctx);
         c = nxt;
@@ -1245,8 +1267,8 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
       return cudaSuccess;
     };
     CK(graph_run(ctx,
-                 gkey("filter", deg, nwb, work_blk, X, Y, Z) + std::string((const char*)&a, sizeof(a)),
-                 filter));
+                 gkey("filter", deg, nwb, work_blk, X, Y, Z, chosen) + std::string((const char*)&a, sizeof(a)),
+                 filter, decided));
     cur = deg % 3;
     if (buf[cur] != X) {
       ctx->last_error = "block filter rotation out of step";
@@ -1406,6 +1428,12 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   // fixed chain per batch layout
   const int repair_cap = (int)(b.c_repair / 2);
   const bool blockm = ctx->prm.eig_mode != GPB_EIG_LANCZOS;
+  // texton variant for this shape bucket: batch pixels and largest side, log2
+  int side = 0;
+  for (size_t i = 0; i < n; i++) side = std::max(side, (int)std::max(ws[i], hs[i]));
+  const std::string tx_key = "texton/px2^" + std::to_string(ilog2(L.total_pix)) + "/side2^" + std::to_string(ilog2(side));
+  bool tx_trial = false;
+  const int tx_var = ctx->tuner.pick(tx_key, kTextonVariants, 1, 1, &tx_trial);
   auto pre_chain = [&]() -> cudaError_t {
     cudaError_t e;
 #define GK(x)                               \
@@ -1415,8 +1443,10 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     // (a) textons
     GK(launch_convert(b.packed, L.total_pix, b.grey, b.lab4, s));
     GK(cudaMemsetAsync(b.repair_count, 0, sizeof(int), s));
+    if (tx_trial) ctx->tuner.begin(tx_key, tx_var, s);
     GK(launch_texton(b.patches, b.work_tex, (int)L.work_tex.size(), b.grey, b.lab4, b.repair, b.repair_count,
-                     repair_cap, s));
+                     repair_cap, s, tx_var));
+    if (tx_trial) ctx->tuner.end(s);
     GK(launch_texton_repair(b.patches, b.grey, b.lab4, b.repair, b.repair_count, repair_cap, ctx->d_k32_ring,
                             ctx->d_ring_of, ctx->tab.n_rings, s));
     GK(stage_mark(ctx->ev[2], s));
@@ -1434,7 +1464,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
                     ctx->prm.keep_intermediates ? b.wfull : nullptr, s));
     if (blockm) {
       GK(cf_launch_full(b.patches, b.work16, (int)L.work16.size(), b.aup, b.adiag, L.lvec, b.afull, s));
-      GK(cudaMemsetAsync(b.berr, 0, sizeof(int), s));
+      GK(cudaMemsetAsync(b.berr, 0, 4 * sizeof(int), s));  // error word and the block step's queue
       ctx->launches++;
     }
     GK(stage_mark(ctx->ev[5], s));
@@ -1443,11 +1473,11 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   };
   CK(graph_run(ctx,
                gkey("pre", L.total_pix, L.lvec, np, L.work_tex.size(), L.work_cue.size(), L.work16.size(),
-                    repair_cap, ctx->tab.n_rings, blockm, ctx->prm.keep_intermediates) +
+                    repair_cap, ctx->tab.n_rings, blockm, ctx->prm.keep_intermediates, tx_var) +
                    gkey("", b.packed, b.grey, b.lab4, b.repair, b.repair_count, b.patches, b.work_tex, b.work_cue,
                         b.work16, b.nbins, b.mpbo, b.go, b.raw, b.counts, b.mpb, b.wup, b.deg, b.aup, b.adiag,
                         b.dis, b.wfull, b.afull, b.berr, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of),
-               pre_chain));
+               pre_chain, !tx_trial));
   // (d) eigensolver
   gpb_status es;
   if (warm) {
@@ -1514,6 +1544,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
                         o_orient, ctx->h_out),
                post_chain));
   CK(cudaStreamSynchronize(s));
+  ctx->tuner.collect();
   if (host_out) {  // staging to the caller's buffers, on the host pool
     std::vector<CopyJob> jobs;
     for (size_t i = 0; i < n; i++) {
@@ -1799,6 +1830,21 @@ extern "C" gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uin
     }
     return GPB_OK;
   });
+}
+
+extern "C" size_t gpb_tuning_report(gpb_ctx* ctx, char* buf, size_t n) {
+  if (!ctx) return 0;
+  try {
+    const std::string r = ctx->tuner.report();
+    if (buf && n) {
+      const size_t m = std::min(n - 1, r.size());
+      memcpy(buf, r.data(), m);
+      buf[m] = 0;
+    }
+    return r.size();
+  } catch (...) {
+    return 0;
+  }
 }
 
 // Accessors for the stages compiled in other translation units.

@@ -117,7 +117,11 @@ struct StepSmem {
   static constexpr size_t c_bytes = (size_t)ST_TY * ST_TX * S::NC * sizeof(float);
   static constexpr size_t stage = y_bytes + c_bytes;  // one pipeline stage
   static constexpr size_t bytes = 2 * stage + 256;    // two stages, tile records, mbarriers
+  // the X-staging variant: one slot per consumer warp for its 4 x 4 block's X rows
+  static constexpr size_t x_slot = (size_t)ST_B * ST_B * kBlk * sizeof(float);
+  static constexpr size_t bytes_xs = bytes + 8 * x_slot;
   static_assert(stage % 128 == 0, "stage alignment");
+  static_assert(bytes_xs <= 232448, "shared memory per CTA");
 };
 
 // what the producer warp tells the consumers about the tile in a stage
@@ -156,6 +160,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
+// 16-byte asynchronous global -> shared copy (L2 only); src_bytes 0 writes
+// zeros and reads nothing
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // polls of the tile's barrier before a CTA gives up (each poll may suspend
 // the thread for a short hardware-defined time; the copies take microseconds)
 constexpr int kBarSpin = 1 << 20;
@@ -244,7 +257,15 @@ __device__ __forceinline__ void step_positions(const float* __restrict__ ys, con
 // a wait that gives up sets *a.err and ends the CTA.
 constexpr int kStepConsumers = 8, kStepThreads = (kStepConsumers + 1) * 32;
 
-template <class S, bool C>
+// Q: the tiles come from a device work queue -- the producer claims the next
+// unclaimed tile with an atomic ticket, so CTAs that meet partial or
+// inactive tiles take more of the others -- instead of a static stride over
+// the list; the last CTA to finish resets the queue for the next launch.
+// XS: the previous iterate X reaches the consumers through shared memory:
+// each warp issues cp.async copies of its block's X rows when a tile starts
+// and waits for them only after the stencil, so their latency never stalls
+// the FMAs (without XS the lanes load X into registers directly).
+template <class S, bool C, bool XS, bool Q>
 __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const int4* __restrict__ work, int nwork,
                                                              const float* __restrict__ Y, const float* __restrict__ X,
                                                              float* __restrict__ out, int step) {
@@ -267,11 +288,23 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
     for (int t = blockIdx.x;; t += gridDim.x, i++) {
       int4 w = make_int4(0, 0, 0, 0);
       bool have = false;
-      for (; t < nwork; t += gridDim.x) {
-        w = work[t];
-        if (a.active[w.x]) {
-          have = true;
-          break;
+      if constexpr (Q) {
+        for (;;) {
+          const int tq = atomicAdd(a.queue, 1);
+          if (tq >= nwork) break;
+          w = work[tq];
+          if (a.active[w.x]) {
+            have = true;
+            break;
+          }
+        }
+      } else {
+        for (; t < nwork; t += gridDim.x) {
+          w = work[t];
+          if (a.active[w.x]) {
+            have = true;
+            break;
+          }
         }
       }
       const int st = i & 1;
@@ -283,6 +316,16 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
       if (!have) {
         m.end = 1;
         mbar_arrive(full + st);
+        if constexpr (Q) {
+          // every claim of this CTA is done; the last CTA to get here resets
+          // the queue (each CTA's claims precede its count in program order)
+          __threadfence();
+          if (atomicAdd(a.queue + 1, 1) == (int)gridDim.x - 1) {
+            a.queue[0] = 0;
+            a.queue[1] = 0;
+            __threadfence();
+          }
+        }
         return;
       }
       const PatchDev P = a.patches[w.x];
@@ -316,6 +359,7 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
   // block columns col, col + 1
   const int by = (warp / (ST_TX / ST_B)) * ST_B + SB_R * (lane >> 4), bx = (warp % (ST_TX / ST_B)) * ST_B;
   const int col = 2 * (lane & 15);
+  float* xslot = (float*)(smem + SM::bytes + (size_t)(warp < kStepConsumers ? warp : 0) * SM::x_slot);
   for (int i = 0;; i++) {
     const int st = i & 1;
     if (!mbar_wait(full + st, (i >> 1) & 1)) {
@@ -329,17 +373,42 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
     // the previous iterate's values for this lane's columns, fetched now so
     // the loads overlap the stencil
     float2 xr[SB_N];
+    if constexpr (XS) {
+      if (m.cz != 0.f) {
+        // the warp's 4 x 4 block: 16 pixel rows of 128 bytes, 128 chunks of 16
+        const int wy = (warp / (ST_TX / ST_B)) * ST_B;
 #pragma unroll
-    for (int k = 0; k < SB_N; k++) {
-      const int y = m.y0 + by + k / SB_C, x = m.x0 + bx + k % SB_C;
-      const bool ok = m.cz != 0.f && y < m.H && x < m.W;
-      xr[k] = ok ? *(const float2*)(X + (m.vec + (long long)y * m.W + x) * kBlk + col) : make_float2(0.f, 0.f);
+        for (int t = 0; t < 4; t++) {
+          const int c = lane + 32 * t, pix = c >> 3, sub = c & 7;
+          const int y = m.y0 + wy + (pix >> 2), x = m.x0 + bx + (pix & 3);
+          const bool ok = y < m.H && x < m.W;
+          cp_async16(xslot + pix * kBlk + sub * 4, ok ? X + (m.vec + (long long)y * m.W + x) * kBlk + sub * 4 : X,
+                     ok ? 16u : 0u);
+        }
+        cp_async_commit();
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < SB_N; k++) {
+        const int y = m.y0 + by + k / SB_C, x = m.x0 + bx + k % SB_C;
+        const bool ok = m.cz != 0.f && y < m.H && x < m.W;
+        xr[k] = ok ? *(const float2*)(X + (m.vec + (long long)y * m.W + x) * kBlk + col) : make_float2(0.f, 0.f);
+      }
     }
     float2 acc[SB_N], lo[SB_N];
     float4 cw[SB_N];
 #pragma unroll
     for (int k = 0; k < SB_N; k++) acc[k] = lo[k] = make_float2(0.f, 0.f);
     step_positions<S, C, 0>(ys + (by * SM::PW + bx) * kBlk + col, cs + (by * ST_TX + bx) * S::NC, cw, acc, lo);
+    if constexpr (XS) {
+      if (m.cz != 0.f) {
+        cp_async_wait_all();
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < SB_N; k++)
+          xr[k] = *(const float2*)(xslot + ((SB_R * (lane >> 4) + k / SB_C) * ST_B + k % SB_C) * kBlk + col);
+      }
+    }
 #pragma unroll
     for (int k = 0; k < SB_N; k++) {
       const int y = m.y0 + by + k / SB_C, x = m.x0 + bx + k % SB_C;
@@ -742,40 +811,55 @@ cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc,
   return cudaGetLastError();
 }
 
-template <class S, bool C>
+template <class S, bool C, bool XS, bool Q>
 static void step_attr() {
-  cudaFuncSetAttribute(cf_step_t<S, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)StepSmem<S>::bytes);
+  cudaFuncSetAttribute(cf_step_t<S, C, XS, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)(XS ? StepSmem<S>::bytes_xs : StepSmem<S>::bytes));
+}
+template <class S, bool C>
+static void step_attrs() {
+  step_attr<S, C, false, false>();
+  step_attr<S, C, true, false>();
+  step_attr<S, C, false, true>();
+  step_attr<S, C, true, true>();
+}
+
+template <class S, bool C>
+static void step_go(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
+                    int step, int grid, int variant, cudaStream_t s) {
+#define GPB_STEP(XS, Q)                                                                                  \
+  cf_step_t<S, C, XS, Q><<<grid, kStepThreads, XS ? StepSmem<S>::bytes_xs : StepSmem<S>::bytes, s>>>( \
+      a, work, nwork, Y, X, out, step)
+  switch (variant & 3) {
+    case 0: GPB_STEP(false, false); break;
+    case 1: GPB_STEP(true, false); break;
+    case 2: GPB_STEP(false, true); break;
+    default: GPB_STEP(true, true); break;
+  }
+#undef GPB_STEP
 }
 
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
-                           int step, cudaStream_t s, bool comp) {
+                           int step, cudaStream_t s, bool comp, int variant) {
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    step_attr<DiskStencil, false>();
-    step_attr<DiskStencil, true>();
-    step_attr<SquareStencil, false>();
-    step_attr<SquareStencil, true>();
+    step_attrs<DiskStencil, false>();
+    step_attrs<DiskStencil, true>();
+    step_attrs<SquareStencil, false>();
+    step_attrs<SquareStencil, true>();
     if (nsm <= 0) nsm = 1;
   }
   const int grid = std::min(nwork, nsm);  // one persistent CTA per SM
   if (grid <= 0) return cudaSuccess;
   if (a.coarse) {
-    if (comp)
-      cf_step_t<SquareStencil, true><<<grid, kStepThreads, StepSmem<SquareStencil>::bytes, s>>>(a, work, nwork, Y, X,
-                                                                                              out, step);
-    else
-      cf_step_t<SquareStencil, false><<<grid, kStepThreads, StepSmem<SquareStencil>::bytes, s>>>(a, work, nwork, Y, X,
-                                                                                               out, step);
+    if (comp) step_go<SquareStencil, true>(a, work, nwork, Y, X, out, step, grid, variant, s);
+    else step_go<SquareStencil, false>(a, work, nwork, Y, X, out, step, grid, variant, s);
   } else {
-    if (comp)
-      cf_step_t<DiskStencil, true><<<grid, kStepThreads, StepSmem<DiskStencil>::bytes, s>>>(a, work, nwork, Y, X, out,
-                                                                                          step);
-    else
-      cf_step_t<DiskStencil, false><<<grid, kStepThreads, StepSmem<DiskStencil>::bytes, s>>>(a, work, nwork, Y, X, out,
-                                                                                           step);
+    if (comp) step_go<DiskStencil, true>(a, work, nwork, Y, X, out, step, grid, variant, s);
+    else step_go<DiskStencil, false>(a, work, nwork, Y, X, out, step, grid, variant, s);
   }
   return cudaGetLastError();
 }

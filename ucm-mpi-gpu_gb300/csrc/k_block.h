@@ -31,6 +31,8 @@ struct BlkArgs {
   int coarse;           // 0: fine radius-5 disk, 1: coarse 7 x 7 square
   const float* afull;   // pixel-major stencil rows: 84 floats (fine) / 52 (coarse)
   int* err;             // set to 1 when a tile's staging wait gave up
+  int* queue;           // [2]: the block step's next tile ticket and finished-CTA
+                        // count; zero between launches (the last CTA resets them)
 };
 
 // coarse level (2 x 2 aggregation)
@@ -55,8 +57,11 @@ cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc,
 void upload_block(const HostTables& t, cudaStream_t s);
 constexpr int kStepTileH = 8, kStepTileW = 16;  // cf_step tile (work list entries)
 constexpr int kFullNC = 84, kCoarseNC = 52;      // floats per pixel-major stencil row
+// variant (bit-identical results, chosen by the autotuner): bit 0 stages X
+// through shared memory, bit 1 takes tiles from the device work queue
+constexpr int kStepVariants = 4, kStepDefault = 1;  // default (untuned): X staged, static tiles
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
-                           int step, cudaStream_t s, bool comp = false);
+                           int step, cudaStream_t s, bool comp = false, int variant = kStepDefault);
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
                            cudaStream_t s);
 cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,

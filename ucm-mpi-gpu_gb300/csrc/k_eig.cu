@@ -105,59 +105,105 @@ __device__ __forceinline__ double patch_sum(const double* part, int tb, int tc, 
   return s;
 }
 
+// Loads are issued in batches -- the stencil by offset for all eight pixels
+// of a thread, the basis by groups of kGrp vectors -- so each thread keeps
+// tens of independent loads in flight; every per-pixel sum still runs in the
+// same order (offsets ascending, basis vectors ascending, pixels ascending).
+// Pixels are addressed by 32-bit offsets into the vector layout, which the
+// host keeps below 2^31 entries.
+constexpr int kGrp = 4;
+
+// h_i = v_i . w for i = 0..j over this thread's pixels, reduced per warp into
+// sred[warp][i]; v_j comes from registers (xj) when given
+__device__ __forceinline__ void basis_dots(const EigArgs& a, int j, const int (&qv)[kEigPix],
+                                           const bool (&okv)[kEigPix], const float (&wv)[kEigPix],
+                                           const float* xj, double* sred, int warp, int lane) {
+  for (int i0 = 0; i0 <= j; i0 += kGrp) {
+    float vv[kGrp][kEigPix];
+#pragma unroll
+    for (int u = 0; u < kGrp; u++) {
+      const int i = i0 + u;
+      const float* Vi = a.V + (long long)i * a.lvec;
+#pragma unroll
+      for (int r = 0; r < kEigPix; r++) vv[u][r] = (i < j || (i == j && !xj)) ? Vi[qv[r]] : (i == j ? xj[r] : 0.f);
+    }
+    float hi[kGrp], lo[kGrp];
+#pragma unroll
+    for (int u = 0; u < kGrp; u++) {
+      hi[u] = lo[u] = 0.f;
+#pragma unroll
+      for (int r = 0; r < kEigPix; r++)
+        if (okv[r]) ff_add_prod(hi[u], lo[u], vv[u][r], wv[r]);
+    }
+#pragma unroll
+    for (int u = 0; u < kGrp; u++) {
+      if (i0 + u > j) break;
+      const double s = ff_warp_reduce(hi[u], lo[u]);
+      if (lane == 0) sred[warp * kRed + i0 + u] = s;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ SpMV
-__global__ void __launch_bounds__(kEigThreads) ks_spmv(EigArgs a, int j, const float* __restrict__ src,
-                                                       int use_beta, float* __restrict__ dst) {
+__global__ void __launch_bounds__(kEigThreads, 2) ks_spmv(EigArgs a, int j, const float* __restrict__ src,
+                                                          int use_beta, float* __restrict__ dst) {
   const EigTile t = a.tiles[blockIdx.x];
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
-  __shared__ long long off[kUpper];
-  if (threadIdx.x < kUpper) off[threadIdx.x] = (long long)c_up_dy[threadIdx.x] * P.W + c_up_dx[threadIdx.x];
+  __shared__ int off[kUpper];
+  if (threadIdx.x < kUpper) off[threadIdx.x] = c_up_dy[threadIdx.x] * P.W + c_up_dx[threadIdx.x];
   __syncthreads();
   const float inv = use_beta ? (float)(1.0 / sqrt(a.beta2[t.patch])) : 1.f;
   const long long base = P.vec;
+  // this thread's pixels; a pixel past the tile reads the tile's first one
+  // (in bounds) and its results are dropped
+  int qv[kEigPix];
+  bool okv[kEigPix];
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) {
+    const int p = t.p0 + threadIdx.x + r * kEigThreads;
+    okv[r] = p < t.p1;
+    qv[r] = (int)(base + (okv[r] ? p : t.p0));
+  }
+  float acc[kEigPix];
+#pragma unroll
+  for (int r = 0; r < kEigPix; r++) acc[r] = 0.f;
+#pragma unroll 2
+  for (int k = 0; k < kUpper; k++) {
+    const float* au = a.a_up + (long long)k * a.lvec;
+    const int o = off[k];
+    float cu[kEigPix], xu[kEigPix], cl[kEigPix], xl[kEigPix];
+#pragma unroll
+    for (int r = 0; r < kEigPix; r++) {
+      cu[r] = au[qv[r]];
+      xu[r] = src[qv[r] + o];
+      cl[r] = au[qv[r] - o];
+      xl[r] = src[qv[r] - o];
+    }
+#pragma unroll
+    for (int r = 0; r < kEigPix; r++) {
+      acc[r] = fmaf(cu[r], xu[r], acc[r]);
+      acc[r] = fmaf(cl[r], xl[r], acc[r]);
+    }
+  }
   float wv[kEigPix], xv[kEigPix];
 #pragma unroll
   for (int r = 0; r < kEigPix; r++) {
-    const int p = t.p0 + threadIdx.x + r * kEigThreads;
-    wv[r] = 0.f;
-    xv[r] = 0.f;
-    if (p >= t.p1) continue;
-    const long long q = base + p;
-    const float x = src[q] * inv;
-    float acc = 0.f;
-#pragma unroll 8
-    for (int k = 0; k < kUpper; k++) {
-      const float* au = a.a_up + (long long)k * a.lvec;
-      acc = fmaf(au[q], src[q + off[k]], acc);
-      acc = fmaf(au[q - off[k]], src[q - off[k]], acc);
-    }
-    xv[r] = x;
-    wv[r] = fmaf(acc, inv, a.a_diag[q] * x);
+    const float x = src[qv[r]] * inv;
+    xv[r] = okv[r] ? x : 0.f;
+    wv[r] = okv[r] ? fmaf(acc[r], inv, a.a_diag[qv[r]] * x) : 0.f;
   }
+  float* Vj = a.V + (long long)j * a.lvec;
 #pragma unroll
   for (int r = 0; r < kEigPix; r++) {
-    const int p = t.p0 + threadIdx.x + r * kEigThreads;
-    if (p >= t.p1) continue;
-    const long long q = base + p;
-    a.V[(long long)j * a.lvec + q] = xv[r];
-    dst[q] = wv[r];
+    if (!okv[r]) continue;
+    Vj[qv[r]] = xv[r];
+    dst[qv[r]] = wv[r];
   }
   // h_i = v_i . w for i <= j
   __shared__ double sred[kEigWarps * kRed];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int i = 0; i <= j; i++) {
-    float hi = 0.f, lo = 0.f;
-#pragma unroll
-    for (int r = 0; r < kEigPix; r++) {
-      const int p = t.p0 + threadIdx.x + r * kEigThreads;
-      if (p >= t.p1) continue;
-      const float v = (i == j) ? xv[r] : a.V[(long long)i * a.lvec + base + p];
-      ff_add_prod(hi, lo, v, wv[r]);
-    }
-    const double s = ff_warp_reduce(hi, lo);
-    if (lane == 0) sred[warp * kRed + i] = s;
-  }
+  basis_dots(a, j, qv, okv, wv, xv, sred, warp, lane);
   cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
   if (last_cta(a.counter + t.patch, a.tile_count[t.patch])) {
     const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
@@ -175,7 +221,7 @@ __global__ void __launch_bounds__(kEigThreads) ks_spmv(EigArgs a, int j, const f
 
 // --------------------------------------------------------------- CGS pass
 // mode 1: w -= V h, then h2 = V^T w;  mode 2: w -= V h2, then |w|^2
-__global__ void __launch_bounds__(kEigThreads) ks_orth(EigArgs a, int j, int mode, float* __restrict__ w) {
+__global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int mode, float* __restrict__ w) {
   const EigTile t = a.tiles[blockIdx.x];
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
@@ -190,22 +236,35 @@ __global__ void __launch_bounds__(kEigThreads) ks_orth(EigArgs a, int j, int mod
     hl[i] = (float)(h - (double)hs[i]);
   }
   __syncthreads();
+  int qv[kEigPix];
+  bool okv[kEigPix];
   float wv[kEigPix], sh[kEigPix], sl[kEigPix];
 #pragma unroll
   for (int r = 0; r < kEigPix; r++) {
     const int p = t.p0 + threadIdx.x + r * kEigThreads;
-    wv[r] = p < t.p1 ? w[base + p] : 0.f;
+    okv[r] = p < t.p1;
+    qv[r] = (int)(base + (okv[r] ? p : t.p0));
+    wv[r] = okv[r] ? w[qv[r]] : 0.f;
     sh[r] = sl[r] = 0.f;
   }
-  for (int i = 0; i <= j; i++) {
-    const float h = hs[i], h2 = hl[i];
+  for (int i0 = 0; i0 <= j; i0 += kGrp) {
+    float vv[kGrp][kEigPix];
 #pragma unroll
-    for (int r = 0; r < kEigPix; r++) {
-      const int p = t.p0 + threadIdx.x + r * kEigThreads;
-      if (p < t.p1) {
-        const float v = a.V[(long long)i * a.lvec + base + p];
-        ff_add_prod(sh[r], sl[r], h, v);
-        sl[r] = fmaf(h2, v, sl[r]);
+    for (int u = 0; u < kGrp; u++) {
+      const float* Vi = a.V + (long long)(i0 + u) * a.lvec;
+#pragma unroll
+      for (int r = 0; r < kEigPix; r++) vv[u][r] = (i0 + u <= j) ? Vi[qv[r]] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kGrp; u++) {
+      if (i0 + u > j) break;
+      const float h = hs[i0 + u], h2 = hl[i0 + u];
+#pragma unroll
+      for (int r = 0; r < kEigPix; r++) {
+        if (okv[r]) {
+          ff_add_prod(sh[r], sl[r], h, vv[u][r]);
+          sl[r] = fmaf(h2, vv[u][r], sl[r]);
+        }
       }
     }
   }
@@ -215,31 +274,21 @@ __global__ void __launch_bounds__(kEigThreads) ks_orth(EigArgs a, int j, int mod
     const float d = wv[r] - sh[r];
     const float z = d - wv[r];
     const float e = (wv[r] - (d - z)) - (sh[r] + z);
-    wv[r] = d + (e - sl[r]);
+    wv[r] = okv[r] ? d + (e - sl[r]) : 0.f;
   }
 #pragma unroll
-  for (int r = 0; r < kEigPix; r++) {
-    const int p = t.p0 + threadIdx.x + r * kEigThreads;
-    if (p < t.p1) w[base + p] = wv[r];
-  }
+  for (int r = 0; r < kEigPix; r++)
+    if (okv[r]) w[qv[r]] = wv[r];
   __shared__ double sred[kEigWarps * kRed];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (mode == 1) {
-    for (int i = 0; i <= j; i++) {
-      float hi = 0.f, lo = 0.f;
-#pragma unroll
-      for (int r = 0; r < kEigPix; r++) {
-        const int p = t.p0 + threadIdx.x + r * kEigThreads;
-        if (p < t.p1) ff_add_prod(hi, lo, a.V[(long long)i * a.lvec + base + p], wv[r]);
-      }
-      const double s = ff_warp_reduce(hi, lo);
-      if (lane == 0) sred[warp * kRed + i] = s;
-    }
+    basis_dots(a, j, qv, okv, wv, nullptr, sred, warp, lane);
     cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
   } else {
     float hi = 0.f, lo = 0.f;
 #pragma unroll
-    for (int r = 0; r < kEigPix; r++) ff_add_prod(hi, lo, wv[r], wv[r]);
+    for (int r = 0; r < kEigPix; r++)
+      if (okv[r]) ff_add_prod(hi, lo, wv[r], wv[r]);
     const double s = ff_warp_reduce(hi, lo);
     if (lane == 0) sred[warp * kRed] = s;
     cta_partials(sred, 1, a.part + (long long)blockIdx.x * a.mp1);

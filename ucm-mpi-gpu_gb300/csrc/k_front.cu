@@ -114,16 +114,19 @@ constexpr int TX_T = 16;              // 16 x 16 outputs per block
 constexpr int TX_W = TX_T + 2 * 24;   // 64
 static_assert(TX_W == 64, "c_goff_off is built for a 64-wide staged tile");
 
-// 64 threads per 16 x 16 tile: a thread owns the 4 pixels (ty0 + 4k, tx),
-// so every offset-table and filter-weight load from constant memory serves
-// four pixels (the kernel is bound by those loads, not by arithmetic)
-constexpr int TX_THREADS = 64, TX_PIX = TX_T * TX_T / TX_THREADS;  // 4 pixels per thread
-
+// TX_THREADS threads per 16 x 16 tile: a thread owns the TX_PIX pixels
+// (ty0 + ROWSTEP k, tx), so every offset-table and filter-weight load from
+// constant memory serves TX_PIX pixels (the kernel is bound by those loads,
+// not by arithmetic).  Each pixel's arithmetic is the same for every thread
+// count, so the variants (32, 64 or 128 threads) give identical labels and
+// the autotuner picks among them.
+template <int TX_THREADS>
 __global__ void __launch_bounds__(TX_THREADS) k_texton(const PatchDev* __restrict__ patches,
                                                        const int4* __restrict__ work,
                                                        const uint8_t* __restrict__ grey,
                                                        uint32_t* __restrict__ lab4, int* __restrict__ repair_list,
                                                        int* __restrict__ repair_count, int repair_cap) {
+  constexpr int TX_PIX = TX_T * TX_T / TX_THREADS;
   __shared__ uint8_t tile[TX_W * TX_W];
   const int4 w = work[blockIdx.x];  // (patch, ty0, tx0, -)
   const PatchDev P = patches[w.x];
@@ -144,7 +147,9 @@ __global__ void __launch_bounds__(TX_THREADS) k_texton(const PatchDev* __restric
     for (int f = 0; f < kNschmid; f++) R[k][f] = E[k][f] = 0.f;
   const uint8_t* c = tile + (ty0 + 24) * TX_W + (tx + 24);
   for (int gi = 0; gi < kSchmidGroups; gi++) {
-    int sum[TX_PIX] = {0, 0, 0, 0};
+    int sum[TX_PIX];
+#pragma unroll
+    for (int k = 0; k < TX_PIX; k++) sum[k] = 0;
     const int e = c_goff_start[gi + 1];
     for (int j = c_goff_start[gi]; j < e; j++) {
       const int off = c_goff_off[j];
@@ -280,9 +285,14 @@ cudaError_t launch_convert(const uint32_t* packed, long long n, uint8_t* grey, u
 
 cudaError_t launch_texton(const PatchDev* patches, const int4* work, int nwork, const uint8_t* grey,
                           uint32_t* lab4, int* repair_list, int* repair_count, int repair_cap,
-                          cudaStream_t s) {
+                          cudaStream_t s, int variant) {
   if (nwork == 0) return cudaSuccess;
-  k_texton<<<nwork, TX_THREADS, 0, s>>>(patches, work, grey, lab4, repair_list, repair_count, repair_cap);
+  if (variant == 0)
+    k_texton<32><<<nwork, 32, 0, s>>>(patches, work, grey, lab4, repair_list, repair_count, repair_cap);
+  else if (variant == 2)
+    k_texton<128><<<nwork, 128, 0, s>>>(patches, work, grey, lab4, repair_list, repair_count, repair_cap);
+  else
+    k_texton<64><<<nwork, 64, 0, s>>>(patches, work, grey, lab4, repair_list, repair_count, repair_cap);
   return cudaGetLastError();
 }
 

@@ -13,9 +13,11 @@ void upload_front(const HostTables& t, cudaStream_t s);
 void upload_codebook(const float* cb, int K, cudaStream_t s);
 cudaError_t launch_convert(const uint32_t* packed, long long n, uint8_t* grey, uint32_t* lab4,
                            cudaStream_t s);
+// variant 0, 1, 2: 32, 64 or 128 threads per 16 x 16 tile (identical labels)
+constexpr int kTextonVariants = 3;
 cudaError_t launch_texton(const PatchDev* patches, const int4* work, int nwork, const uint8_t* grey,
                           uint32_t* lab4, int* repair_list, int* repair_count, int repair_cap,
-                          cudaStream_t s);
+                          cudaStream_t s, int variant = 1);
 cudaError_t launch_texton_repair(const PatchDev* patches, const uint8_t* grey, uint32_t* lab4,
                                  const int* repair_list, const int* repair_count, int repair_cap,
                                  const double* k32_ring, const int* ring_of, int n_rings,

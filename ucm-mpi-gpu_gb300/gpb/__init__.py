@@ -107,6 +107,8 @@ def _lib():
         L.gpb_fetch.restype = c
         L.gpb_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
         L.gpb_last_stats.restype = c
+        L.gpb_tuning_report.argtypes = [vp, ctypes.c_char_p, sz]
+        L.gpb_tuning_report.restype = sz
         L.gpb_device_count.restype = c
         L.gpb_status_str.argtypes = [c]
         L.gpb_status_str.restype = ctypes.c_char_p
@@ -233,6 +235,21 @@ class Context:
         self._ck(st, "gpb_compute_batch_device", allow_noconv=True)
         self.last_status = st
         return st
+
+    def tuning_report(self):
+        """gpb_tuning_report: the autotuner's choice per shape bucket, as a dict
+        key -> (chosen variant, [median ms per variant])."""
+        n = _lib().gpb_tuning_report(self._h, None, 0)
+        buf = ctypes.create_string_buffer(n + 1)
+        _lib().gpb_tuning_report(self._h, buf, n + 1)
+        out = {}
+        for item in buf.value.decode().split("; "):
+            if "=" not in item:
+                continue
+            k, rest = item.split("=", 1)
+            ch, ms = rest.split(" (", 1)
+            out[k] = (int(ch), [float(x) for x in ms.rstrip(")").split()])
+        return out
 
     def fetch(self, stage, patch, shape, dtype):
         out = np.empty(shape, dtype)
