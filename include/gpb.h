@@ -56,7 +56,9 @@ typedef enum {
   GPB_EIG_LANCZOS = 0,   /* plain cold-start thick-restart Lanczos (Krylov-Schur) */
   GPB_EIG_WARM = 1,      /* block Chebyshev-filtered solver warm-started from the
                             2x2-aggregated (coarse) problem                       */
-  GPB_EIG_BLOCK = 2      /* the same block solver from a seeded random start      */
+  GPB_EIG_BLOCK = 2,     /* the same block solver from a seeded random start      */
+  GPB_EIG_LEARNED = 3    /* the same block solver started from the learned
+                            network's 32 fields (gpb_learned_set)                */
 } gpb_eig_mode;
 
 typedef struct {
@@ -130,7 +132,8 @@ typedef enum {
   /* float H*W*9, gpb_warmnet_capture on: the first 9 columns of the
    * warm-start block (prolongated coarse Ritz vectors), pixel-major, before
    * the learned correction */
-  GPB_STAGE_WARM0 = 11
+  GPB_STAGE_WARM0 = 11,
+  GPB_STAGE_DEG = 12      /* float  H*W   affinity degree sum_q W(p,q) */
 } gpb_stage;
 
 void gpb_default_params(gpb_params* p);
@@ -356,6 +359,41 @@ gpb_status gpb_warmnet_capture(gpb_ctx* ctx, int on);
 gpb_status gpb_warmnet_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
                                    const float* d_xt, const float* d_mpb, const float* d_vt, const float* weights,
                                    double* loss, float* grad);
+
+/* ---- Learned warm start (GPB_EIG_LEARNED) -----------------------------
+ * A 4-level convolutional encoder-decoder maps each patch's mPb and
+ * affinity degree (/81), per pixel, to 32 fields that start the block
+ * eigensolver in place of a random block or the coarse-grid solve.  3 x 3
+ * convolutions with channels 16/32/64/64 per level, 2 x 2 mean pooling,
+ * nearest up-sampling with skip concatenation, ReLU, a 16 -> 32 head: BF16
+ * weights and activations on the tensor cores, FP32 accumulation.  The
+ * parameters (gpb_learned_nparams() FP32 values) are, per convolution in
+ * the order e0a e0b e1a e1b e2a e2b e3a e3b d2a d2b d1a d1b d0a d0b head,
+ * W[cout][3][3][cin] then b[cout].  Training minimises, per patch,
+ * 9 - tr(V^T P_Y V): the energy of the 9 eigenvectors V the plain solver
+ * finds outside the span of the 32 fields Y.  The solve itself still
+ * iterates to eig_tol, and a block solve that fails falls back to plain
+ * Lanczos.  No counterpart in the reference.
+ *
+ * The _device calls take n patches by their sizes and device arrays holding
+ * them back to back: mPb and degree [H*W] each, targets V [H*W][9], fields
+ * Y [H*W][32]. */
+size_t gpb_learned_nparams(void);
+/* the weights (n = gpb_learned_nparams()); NULL drops them */
+gpb_status gpb_learned_set(gpb_ctx* ctx, const float* params, size_t n);
+gpb_status gpb_learned_get(gpb_ctx* ctx, float* params, size_t n);
+gpb_status gpb_learned_forward_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                      const float* d_mpb, const float* d_deg, float* d_y);
+/* the loss summed over the patches and its gradient (host, parameter layout) */
+gpb_status gpb_learned_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                   const float* d_mpb, const float* d_deg, const float* d_v, double* loss,
+                                   float* grad);
+/* Adam (beta 0.9 / 0.999) on the context's weights over `epochs` passes of
+ * the n patches in seeded random minibatches of `batch` patches; the mean
+ * loss per patch of each epoch into loss_per_epoch (host, `epochs`). */
+gpb_status gpb_learned_train_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                    const float* d_mpb, const float* d_deg, const float* d_v, int batch, int epochs,
+                                    float lr, uint64_t seed, double* loss_per_epoch);
 
 int gpb_device_count(void);
 const char* gpb_status_str(gpb_status s);

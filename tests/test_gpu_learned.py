@@ -1,0 +1,119 @@
+"""The learned warm start's network on the GPU (BF16 tensor cores, FP32
+accumulation) against its FP64 oracle, which rounds to bfloat16 where the
+kernels store or feed values to the tensor cores: the forward fields, the
+subspace loss and every parameter's gradient.  Then training lowers the
+loss, and the trained network, as the start of the block eigensolver, is
+checked for its gain on held-out patches."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _lo():
+    import learned_oracle
+    return learned_oracle
+
+
+def _inputs(seed, shapes):
+    """smooth-ish mPb in [0, 1], degree in [1, 81] and 9 orthonormal targets"""
+    rng = np.random.default_rng(seed)
+    out = []
+    for (H, W) in shapes:
+        mpb = np.clip(rng.normal(0.2, 0.2, (H, W)), 0, 1)
+        deg = rng.uniform(5, 81, (H, W))
+        v, _ = np.linalg.qr(rng.normal(size=(H * W, 9)))
+        out.append((mpb, deg, v))
+    return out
+
+
+def _dev(torch, arrs):
+    return torch.from_numpy(np.concatenate([np.ascontiguousarray(a, np.float32).ravel() for a in arrs])).cuda()
+
+
+def _params(seed):
+    lo = _lo()
+    p = lo.init_params(seed)
+    lay, _ = lo.param_layout()
+    rng = np.random.default_rng(seed + 1)
+    for _, _, bo, _, co in lay:
+        p[bo:bo + co] = rng.normal(0, 0.02, co)
+    return p
+
+
+SHAPES = [(37, 29), (24, 40), (16, 16)]
+
+
+def test_forward_matches_oracle():
+    torch = pytest.importorskip("torch")
+    import gpb
+    lo = _lo()
+    data = _inputs(3, SHAPES)
+    p = _params(5)
+    ctx = gpb.Context()
+    ctx.learned_set(p)
+    assert np.array_equal(ctx.learned_get(), p)
+    d_m, d_d = _dev(torch, [d[0] for d in data]), _dev(torch, [d[1] for d in data])
+    total = sum(H * W for H, W in SHAPES)
+    d_y = torch.zeros(total * lo.NOUT, dtype=torch.float32, device="cuda")
+    ctx.learned_forward_device(SHAPES, d_m.data_ptr(), d_d.data_ptr(), d_y.data_ptr())
+    y = d_y.cpu().numpy().astype(np.float64)
+    at = 0
+    for (H, W), (mpb, deg, _) in zip(SHAPES, data):
+        want = lo.forward(p, lo.features(mpb, deg), bf=True)
+        got = y[at * lo.NOUT:(at + H * W) * lo.NOUT].reshape(H, W, lo.NOUT)
+        rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+        assert rel < 1e-2, rel
+        at += H * W
+    ctx.close()
+
+
+def test_loss_and_gradient_match_oracle():
+    """The CUDA kernels' loss and gradient of every parameter against the
+    oracle's backward pass (bfloat16 at the same places): the whole gradient
+    within 2% relative, each convolution's within 5%."""
+    torch = pytest.importorskip("torch")
+    import gpb
+    lo = _lo()
+    data = _inputs(7, SHAPES)
+    p = _params(9)
+    ctx = gpb.Context()
+    ctx.learned_set(p)
+    d_m, d_d = _dev(torch, [d[0] for d in data]), _dev(torch, [d[1] for d in data])
+    d_v = _dev(torch, [d[2] for d in data])
+    loss, g = ctx.learned_grad_device(SHAPES, d_m.data_ptr(), d_d.data_ptr(), d_v.data_ptr())
+    ctx.close()
+    want_loss, want_g = 0.0, np.zeros(lo.nparams())
+    for (H, W), (mpb, deg, v) in zip(SHAPES, data):
+        f = lo.features(mpb, deg)
+        y = lo.forward(p, f, bf=True)
+        L, dy = lo.subspace_loss(y, v.reshape(H, W, 9), grad=True)
+        want_loss += L
+        want_g += lo.backward(p, f, dy, bf=True)
+    assert abs(loss - want_loss) < 1e-3 * max(1.0, want_loss), (loss, want_loss)
+    assert np.linalg.norm(g - want_g) / np.linalg.norm(want_g) < 2e-2
+    lay, _ = lo.param_layout()
+    for name, wo, bo, ci, co in lay:
+        gw, ww = g[wo:bo + co], want_g[wo:bo + co]
+        assert np.linalg.norm(gw - ww) / np.linalg.norm(ww) < 5e-2, name
+
+
+def test_training_lowers_the_loss():
+    """A few epochs of the library's own Adam on the GPU on eigenvectors the
+    plain solver finds for small synthetic patches."""
+    torch = pytest.importorskip("torch")
+    import gpb
+    from gpb import learned
+    lo = _lo()
+    shapes, mpb, deg, v = learned.make_dataset(12, 64, seed=11)
+    ctx = gpb.Context()
+    ctx.learned_set(lo.init_params(0))
+    hist = ctx.learned_train_device(shapes, mpb.data_ptr(), deg.data_ptr(), v.data_ptr(), batch=4, epochs=6,
+                                    lr=2e-3, seed=1)
+    assert np.all(np.isfinite(hist))
+    assert hist[-1] < 0.8 * hist[0], hist
+    ctx.close()

@@ -29,6 +29,7 @@
 #include "gpb_internal.h"
 #include "host_pool.h"
 #include "k_block.h"
+#include "k_learned.h"
 #include "k_warmnet.h"
 #include "k_eig.h"
 #include "k_static.h"
@@ -193,6 +194,12 @@ struct gpb_ctx {
   bool use_graphs = true;
   // kernel variants chosen per shape bucket (autotune.h)
   Autotuner tuner;
+  // the learned warm start's network (k_learned.cu), and the device staging
+  // of a training minibatch
+  std::unique_ptr<LearnedNet> net;
+  float *d_tr = nullptr;
+  size_t c_tr = 0;
+  int learned_launches = 0;
   std::unique_ptr<HostPool> pool;
   HostPool& host_pool() {
     if (!pool) pool.reset(new HostPool(std::max(1u, std::min(16u, std::thread::hardware_concurrency()))));
@@ -418,7 +425,7 @@ extern "C" gpb_status gpb_create(gpb_ctx** out, const gpb_params* p) {
     else gpb_default_params(&ctx->prm);
     gpb_params& q = ctx->prm;
     if (q.nvec < 2 || q.nvec > kMaxNvec || q.krylov_dim > kMaxKrylov || q.krylov_keep >= q.krylov_dim ||
-        q.krylov_keep < q.nvec || !(q.eig_tol > 0) || q.eig_mode < GPB_EIG_LANCZOS || q.eig_mode > GPB_EIG_BLOCK ||
+        q.krylov_keep < q.nvec || !(q.eig_tol > 0) || q.eig_mode < GPB_EIG_LANCZOS || q.eig_mode > GPB_EIG_LEARNED ||
         (q.eig_mode != GPB_EIG_LANCZOS && q.nvec > kBlk) || (q.eig_mode == GPB_EIG_WARM && !(q.warm_tol > 0))) {
       delete ctx;
       return GPB_ERR_ARG;
@@ -509,6 +516,8 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
   cudaFree(ctx->d_wn_x0);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   drop_graphs(ctx);
+  ctx->net.reset();
+  if (ctx->d_tr) cudaFree(ctx->d_tr);
   {
     ConstBank& bk = bank_of(ctx->device);
     std::lock_guard<std::mutex> lk(bk.mu);
@@ -1356,6 +1365,33 @@ static gpb_status solve_warm(gpb_ctx* ctx, const Layout& L, const Layout& Lc) {
   return solve_block(ctx, lf, true, ctx->prm.eig_tol, true, &Xf);
 }
 
+// block solve started from the learned network's fields
+static gpb_status solve_learned(gpb_ctx* ctx, const Layout& L) {
+  Buf& b = ctx->b;
+  cudaStream_t s = ctx->st;
+  if (!ctx->net || !ctx->net->has_params()) {
+    ctx->last_error = "GPB_EIG_LEARNED needs the network's weights (gpb_learned_set)";
+    return GPB_ERR_ARG;
+  }
+  std::vector<int> H, W;
+  int maxn = 0;
+  for (const PatchDev& P : L.patches) {
+    H.push_back(P.H);
+    W.push_back(P.W);
+    maxn = std::max(maxn, P.N);
+  }
+  const int l0 = ctx->net->launches();
+  CK(ctx->net->layout(H, W, s));
+  CK(ctx->net->features_from(b.patches, b.mpb, b.deg, s));
+  CK(ctx->net->forward(s));
+  CK(ln_launch_start(ctx->net->patches0_dev(), b.patches, (int)L.patches.size(), maxn, ctx->net->y(), b.blk[0], s));
+  ctx->launches += ctx->net->launches() - l0 + 1;
+  Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.afull, 0,
+              {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
+  float* Xf = nullptr;
+  return solve_block(ctx, lf, true, ctx->prm.eig_tol, true, &Xf);
+}
+
 static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const uint32_t* hs,
                             const uint32_t* const* host_in, const size_t* host_stride, const uint32_t* dev_in,
                             const size_t* dev_off, float* dev_nmax, float* dev_orient, gpb_result* host_out) {
@@ -1482,6 +1518,8 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   gpb_status es;
   if (warm) {
     es = solve_warm(ctx, L, Lc);
+  } else if (ctx->prm.eig_mode == GPB_EIG_LEARNED) {
+    es = solve_learned(ctx, L);
   } else if (ctx->prm.eig_mode == GPB_EIG_BLOCK) {
     Level lf = {&L, b.patches, b.tiles, b.tile_begin, b.tile_count, b.work_blk, b.afull, 0,
                 {b.blk[0], b.blk[1], b.blk[2], b.blk[3]}};
@@ -1676,6 +1714,10 @@ extern "C" gpb_status gpb_fetch(gpb_ctx* ctx, int stage, size_t patch, void* dst
         if (!need(N * 4)) return GPB_ERR_ARG;
         e = cudaMemcpy(dst, b.mpb + P.pix, N * 4, cudaMemcpyDeviceToHost);
         break;
+      case GPB_STAGE_DEG:
+        if (!need(N * 4)) return GPB_ERR_ARG;
+        e = cudaMemcpy(dst, b.deg + P.vec, N * 4, cudaMemcpyDeviceToHost);
+        break;
       case GPB_STAGE_W:
         if (!b.wfull || !need(81 * N * 4)) return GPB_ERR_ARG;
         e = cudaMemcpy(dst, b.wfull + 81 * P.pix, 81 * N * 4, cudaMemcpyDeviceToHost);
@@ -1828,6 +1870,154 @@ extern "C" gpb_status gpb_texton_labels_static(gpb_ctx* ctx, uint32_t width, uin
       CK(cudaEventRecord(bk.static_done, s));
       bk.static_pending = true;
     }
+    return GPB_OK;
+  });
+}
+
+extern "C" size_t gpb_learned_nparams(void) { return ln_nparams(); }
+
+static LearnedNet& net_of(gpb_ctx* ctx) {
+  if (!ctx->net) ctx->net.reset(new LearnedNet());
+  return *ctx->net;
+}
+
+extern "C" gpb_status gpb_learned_set(gpb_ctx* ctx, const float* params, size_t n) {
+  if (!ctx) return GPB_ERR_ARG;
+  return guarded(ctx, [&]() -> gpb_status {
+    CK(cudaSetDevice(ctx->device));
+    if (!params) {
+      CK(cudaStreamSynchronize(ctx->st));
+      ctx->net.reset();
+      return GPB_OK;
+    }
+    if (n != ln_nparams()) return GPB_ERR_ARG;
+    CK(net_of(ctx).set_params(params, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return GPB_OK;
+  });
+}
+
+extern "C" gpb_status gpb_learned_get(gpb_ctx* ctx, float* params, size_t n) {
+  if (!ctx || !params || n != ln_nparams()) return GPB_ERR_ARG;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx->net || !ctx->net->has_params()) return GPB_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->net->get_params(params, ctx->st));
+    return GPB_OK;
+  });
+}
+
+static gpb_status learned_layout(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights) {
+  if (!ctx->net || !ctx->net->has_params() || n == 0 || !widths || !heights) return GPB_ERR_ARG;
+  std::vector<int> H(n), W(n);
+  for (size_t i = 0; i < n; i++) {
+    if (widths[i] < 1 || heights[i] < 1 || widths[i] > 8192 || heights[i] > 8192) return GPB_ERR_ARG;
+    H[i] = (int)heights[i];
+    W[i] = (int)widths[i];
+  }
+  CK(cudaSetDevice(ctx->device));
+  CK(ctx->net->layout(H, W, ctx->st));
+  return GPB_OK;
+}
+
+extern "C" gpb_status gpb_learned_forward_device(gpb_ctx* ctx, size_t n, const uint32_t* widths,
+                                                 const uint32_t* heights, const float* d_mpb, const float* d_deg,
+                                                 float* d_y) {
+  if (!ctx || !d_mpb || !d_deg || !d_y) return GPB_ERR_ARG;
+  return guarded(ctx, [&]() -> gpb_status {
+    gpb_status st = learned_layout(ctx, n, widths, heights);
+    if (st != GPB_OK) return st;
+    cudaStream_t s = ctx->st;
+    CK(ctx->net->features(d_mpb, d_deg, s));
+    CK(ctx->net->forward(s));
+    CK(cudaMemcpyAsync(d_y, ctx->net->y(), (size_t)ctx->net->npix0() * kLnOut * sizeof(float),
+                       cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return GPB_OK;
+  });
+}
+
+extern "C" gpb_status gpb_learned_grad_device(gpb_ctx* ctx, size_t n, const uint32_t* widths, const uint32_t* heights,
+                                              const float* d_mpb, const float* d_deg, const float* d_v, double* loss,
+                                              float* grad) {
+  if (!ctx || !d_mpb || !d_deg || !d_v || !loss || !grad) return GPB_ERR_ARG;
+  return guarded(ctx, [&]() -> gpb_status {
+    gpb_status st = learned_layout(ctx, n, widths, heights);
+    if (st != GPB_OK) return st;
+    cudaStream_t s = ctx->st;
+    CK(ctx->net->features(d_mpb, d_deg, s));
+    CK(ctx->net->forward(s));
+    CK(ctx->net->loss_backward(d_v, loss, s));
+    CK(cudaMemcpyAsync(grad, ctx->net->grad(), ln_nparams() * sizeof(float), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return GPB_OK;
+  });
+}
+
+extern "C" gpb_status gpb_learned_train_device(gpb_ctx* ctx, size_t n, const uint32_t* widths,
+                                               const uint32_t* heights, const float* d_mpb, const float* d_deg,
+                                               const float* d_v, int batch, int epochs, float lr, uint64_t seed,
+                                               double* loss_per_epoch) {
+  if (!ctx || !d_mpb || !d_deg || !d_v || !widths || !heights || n == 0 || batch < 1 || epochs < 1 || !(lr > 0))
+    return GPB_ERR_ARG;
+  return guarded(ctx, [&]() -> gpb_status {
+    if (!ctx->net || !ctx->net->has_params()) return GPB_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->st;
+    std::vector<long long> off(n + 1, 0);
+    for (size_t i = 0; i < n; i++) off[i + 1] = off[i] + (long long)widths[i] * heights[i];
+    // staging of one minibatch: mPb, degree and targets, back to back
+    long long most = 0;
+    {
+      std::vector<long long> sz(n);
+      for (size_t i = 0; i < n; i++) sz[i] = off[i + 1] - off[i];
+      std::sort(sz.begin(), sz.end(), std::greater<long long>());
+      for (int i = 0; i < batch && i < (int)n; i++) most += sz[i];
+    }
+    CK(grow(ctx->d_tr, ctx->c_tr, (size_t)most * (2 + kLnTargets)));
+    std::vector<int> order(n);
+    for (size_t i = 0; i < n; i++) order[i] = (int)i;
+    uint64_t rs = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto rnd = [&]() {
+      rs = rs * 6364136223846793005ULL + 1442695040888963407ULL;
+      return (uint32_t)(rs >> 33);
+    };
+    int t = 0;
+    for (int ep = 0; ep < epochs; ep++) {
+      for (size_t i = n - 1; i > 0; i--) std::swap(order[i], order[rnd() % (i + 1)]);
+      double ep_loss = 0;
+      for (size_t b0 = 0; b0 < n; b0 += batch) {
+        const size_t nb = std::min(n - b0, (size_t)batch);
+        std::vector<uint32_t> bw(nb), bh(nb);
+        long long tot = 0;
+        for (size_t k = 0; k < nb; k++) tot += off[order[b0 + k] + 1] - off[order[b0 + k]];
+        float* m_mpb = ctx->d_tr;
+        float* m_deg = m_mpb + tot;
+        float* m_v = m_deg + tot;
+        long long at = 0;
+        for (size_t k = 0; k < nb; k++) {
+          const int i = order[b0 + k];
+          const long long N = off[i + 1] - off[i];
+          bw[k] = widths[i];
+          bh[k] = heights[i];
+          CK(cudaMemcpyAsync(m_mpb + at, d_mpb + off[i], N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+          CK(cudaMemcpyAsync(m_deg + at, d_deg + off[i], N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+          CK(cudaMemcpyAsync(m_v + at * kLnTargets, d_v + off[i] * kLnTargets, N * kLnTargets * sizeof(float),
+                             cudaMemcpyDeviceToDevice, s));
+          at += N;
+        }
+        gpb_status st = learned_layout(ctx, nb, bw.data(), bh.data());
+        if (st != GPB_OK) return st;
+        double l = 0;
+        CK(ctx->net->features(m_mpb, m_deg, s));
+        CK(ctx->net->forward(s));
+        CK(ctx->net->loss_backward(m_v, &l, s));
+        CK(ctx->net->adam(lr, 0.9f, 0.999f, 1e-8f, ++t, s));
+        ep_loss += l;
+      }
+      if (loss_per_epoch) loss_per_epoch[ep] = ep_loss / (double)n;
+    }
+    CK(cudaStreamSynchronize(s));
     return GPB_OK;
   });
 }

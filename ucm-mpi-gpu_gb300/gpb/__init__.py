@@ -23,9 +23,9 @@ STATIC_MAX_PIXELS = 1 << 20   # gpb_texton_labels_static's scratch limit
 STITCH_LAST, STITCH_INTERIOR, STITCH_BLEND = 0, 1, 2
 UCM_QUANT, UCM_ARCS, UCM_WSWT, UCM_WSWT2, UCM_REGIONS = range(5)
 COMPAT_CPU, COMPAT_DAMASCENE = 0, 1
-EIG_LANCZOS, EIG_WARM, EIG_BLOCK = 0, 1, 2
+EIG_LANCZOS, EIG_WARM, EIG_BLOCK, EIG_LEARNED = 0, 1, 2, 3
 STAGES = {"texton": 0, "labbins": 1, "mpb_o": 2, "mpb": 3, "W": 4, "evals": 5, "evecs": 6,
-          "spb": 7, "cues": 8, "gpb_o": 9, "counts": 10, "warm0": 11}
+          "spb": 7, "cues": 8, "gpb_o": 9, "counts": 10, "warm0": 11, "deg": 12}
 WARMNET_PARAMS = 1609
 
 
@@ -109,6 +109,18 @@ def _lib():
         L.gpb_last_stats.restype = c
         L.gpb_tuning_report.argtypes = [vp, ctypes.c_char_p, sz]
         L.gpb_tuning_report.restype = sz
+        L.gpb_learned_nparams.restype = sz
+        L.gpb_learned_set.argtypes = [vp, vp, sz]
+        L.gpb_learned_set.restype = c
+        L.gpb_learned_get.argtypes = [vp, vp, sz]
+        L.gpb_learned_get.restype = c
+        L.gpb_learned_forward_device.argtypes = [vp, sz, vp, vp, vp, vp, vp]
+        L.gpb_learned_forward_device.restype = c
+        L.gpb_learned_grad_device.argtypes = [vp, sz, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_double), vp]
+        L.gpb_learned_grad_device.restype = c
+        L.gpb_learned_train_device.argtypes = [vp, sz, vp, vp, vp, vp, vp, c, c, ctypes.c_float, ctypes.c_uint64,
+                                               vp]
+        L.gpb_learned_train_device.restype = c
         L.gpb_device_count.restype = c
         L.gpb_status_str.argtypes = [c]
         L.gpb_status_str.restype = ctypes.c_char_p
@@ -154,6 +166,10 @@ def default_params(**kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+def learned_nparams():
+    return int(_lib().gpb_learned_nparams())
 
 
 def device_count():
@@ -235,6 +251,53 @@ class Context:
         self._ck(st, "gpb_compute_batch_device", allow_noconv=True)
         self.last_status = st
         return st
+
+    # ---- learned warm start (GPB_EIG_LEARNED)
+    def learned_set(self, params):
+        """gpb_learned_set: the network's weights (float32, learned_nparams());
+        None drops them."""
+        if params is None:
+            self._ck(_lib().gpb_learned_set(self._h, None, 0), "gpb_learned_set")
+            return
+        w = np.ascontiguousarray(params, np.float32)
+        self._ck(_lib().gpb_learned_set(self._h, w.ctypes.data, w.size), "gpb_learned_set")
+
+    def learned_get(self):
+        w = np.empty(learned_nparams(), np.float32)
+        self._ck(_lib().gpb_learned_get(self._h, w.ctypes.data, w.size), "gpb_learned_get")
+        return w
+
+    @staticmethod
+    def _sizes(shapes):
+        h = np.ascontiguousarray([s[0] for s in shapes], np.uint32)
+        w = np.ascontiguousarray([s[1] for s in shapes], np.uint32)
+        return w, h
+
+    def learned_forward_device(self, shapes, d_mpb, d_deg, d_y):
+        """the 32 fields [H*W][32] per patch into device memory d_y; shapes:
+        (H, W) per patch; d_mpb, d_deg: device arrays of H*W per patch."""
+        w, h = self._sizes(shapes)
+        self._ck(_lib().gpb_learned_forward_device(self._h, len(shapes), w.ctypes.data, h.ctypes.data, d_mpb, d_deg,
+                                                   d_y), "gpb_learned_forward_device")
+
+    def learned_grad_device(self, shapes, d_mpb, d_deg, d_v):
+        """(loss summed over the patches, gradient) for the current weights."""
+        w, h = self._sizes(shapes)
+        loss = ctypes.c_double()
+        g = np.empty(learned_nparams(), np.float32)
+        self._ck(_lib().gpb_learned_grad_device(self._h, len(shapes), w.ctypes.data, h.ctypes.data, d_mpb, d_deg,
+                                                d_v, ctypes.byref(loss), g.ctypes.data), "gpb_learned_grad_device")
+        return loss.value, g
+
+    def learned_train_device(self, shapes, d_mpb, d_deg, d_v, batch, epochs, lr, seed=0):
+        """Adam on the context's weights; returns the mean loss per patch of
+        each epoch."""
+        w, h = self._sizes(shapes)
+        hist = np.zeros(epochs, np.float64)
+        self._ck(_lib().gpb_learned_train_device(self._h, len(shapes), w.ctypes.data, h.ctypes.data, d_mpb, d_deg,
+                                                 d_v, batch, epochs, lr, seed, hist.ctypes.data),
+                 "gpb_learned_train_device")
+        return hist
 
     def tuning_report(self):
         """gpb_tuning_report: the autotuner's choice per shape bucket, as a dict

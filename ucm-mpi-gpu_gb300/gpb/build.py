@@ -19,7 +19,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
           "-I" + CSRC, "-I" + os.path.join(os.path.dirname(ROOT), "include")]
 SOURCES = ["tables.cpp", "eig_host.cpp", "gpb_api.cpp", "gpb_damascene.cpp", "io_writers.cpp", "k_block.cu",
            "k_front.cu", "k_static.cu", "k_stitch.cu", "k_spfeat.cu", "k_cues.cu", "k_buildw.cu", "k_eig.cu", "k_spb.cu",
-           "ucm_host.cpp", "ucm_api.cpp", "k_ucm.cu", "k_warmnet.cu"]
+           "ucm_host.cpp", "ucm_api.cpp", "k_ucm.cu", "k_warmnet.cu", "k_learned.cu"]
 
 
 def nvcc():
