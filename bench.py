@@ -341,7 +341,8 @@ def run_gpu(args):
     # timed with events on the library stream in a profiled run
     os.environ["GPB_PROFILE"] = "1"
     pctx = gpb.Context(cb, eig_mode=gpb.EIG_WARM)
-    pctx.compute_batch_device(ws, hs, offs, d_in.data_ptr(), d_nmax.data_ptr(), d_orient.data_ptr())
+    for _ in range(2):  # the second call runs the tuned variants only
+        pctx.compute_batch_device(ws, hs, offs, d_in.data_ptr(), d_nmax.data_ptr(), d_orient.data_ptr())
     ps = pctx.stats()
     os.environ.pop("GPB_PROFILE")
     pctx.close()

@@ -67,7 +67,7 @@ def test_autotuner_settles_and_keeps_results(mode):
     assert ref.tuning_report() == {}
     ref.close()
     ctx = gpb.Context(cb, eig_mode=mode)
-    for call in range(4):  # texton has 3 variants, one trial per call
+    for call in range(4):  # the texton variants are all tried within the first call
         got = ctx.compute_batch(patches)
         for (nm_a, or_a), (nm_b, or_b) in zip(want, got):
             assert np.array_equal(nm_a, nm_b) and np.array_equal(or_a, or_b), call
@@ -75,7 +75,9 @@ def test_autotuner_settles_and_keeps_results(mode):
     tex = [k for k in rep if k.startswith("texton/")]
     steps = [k for k in rep if k.startswith("step/")]
     assert tex and steps, rep
-    for k in tex:
-        assert rep[k][0] in (0, 1, 2) and len(rep[k][1]) == 3 and min(rep[k][1]) > 0, rep[k]
+    for k in tex:  # timed trials, or settled on the default for too few tiles
+        ms = rep[k][1]
+        assert rep[k][0] in (0, 1, 2) and len(ms) == 3, rep[k]
+        assert min(ms) > 0 or (rep[k][0] == 1 and max(ms) < 0), rep[k]
     assert any(rep[k][0] >= 0 for k in steps), rep
     ctx.close()

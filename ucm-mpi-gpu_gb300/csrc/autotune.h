@@ -68,11 +68,22 @@ class Autotuner {
     return it != tab_.end() && it->second.chosen >= 0;
   }
 
-  // events around a trial launch of variant v
-  void begin(const std::string& key, int v, cudaStream_t s) {
-    Pending p{key, v, take(), take()};
+  // events around a trial launch of variant v; its time counts `scale`
+  // times (a trial on 1/scale of a launch's independent work items)
+  void begin(const std::string& key, int v, cudaStream_t s, float scale = 1.f) {
+    Pending p{key, v, take(), take(), scale};
     cudaEventRecord(p.a, s);
     pend_.push_back(p);
+  }
+  // registers a key and decides it at once (no trials worth timing)
+  void settle(const std::string& key, int nvar, int v) {
+    Entry& e = tab_[key];
+    if (e.nvar == 0) {
+      e.nvar = nvar;
+      e.ms.assign(nvar, {});
+      e.issued.assign(nvar, 0);
+    }
+    if (e.chosen < 0) e.chosen = v;
   }
   void end(cudaStream_t s) {
     if (!pend_.empty()) cudaEventRecord(pend_.back().b, s);
@@ -83,7 +94,7 @@ class Autotuner {
   void collect() {
     for (auto& p : pend_) {
       float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) tab_[p.key].ms[p.v].push_back(ms);
+      if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) tab_[p.key].ms[p.v].push_back(ms * p.scale);
       free_.push_back(p.a);
       free_.push_back(p.b);
     }
@@ -136,6 +147,7 @@ class Autotuner {
     std::string key;
     int v;
     cudaEvent_t a, b;
+    float scale;
   };
   cudaEvent_t take() {
     if (!free_.empty()) {

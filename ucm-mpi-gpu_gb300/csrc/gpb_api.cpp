@@ -1468,8 +1468,15 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   int side = 0;
   for (size_t i = 0; i < n; i++) side = std::max(side, (int)std::max(ws[i], hs[i]));
   const std::string tx_key = "texton/px2^" + std::to_string(ilog2(L.total_pix)) + "/side2^" + std::to_string(ilog2(side));
-  bool tx_trial = false;
-  const int tx_var = ctx->tuner.pick(tx_key, kTextonVariants, 1, 1, &tx_trial);
+  // an undecided bucket tries every variant within this one launch, each on
+  // a third of the tile list (the tiles are independent and the labels the
+  // same), timed and scaled to the whole list
+  const int ntex = (int)L.work_tex.size();
+  if (ctx->tuner.enabled && !ctx->tuner.decided(tx_key) && ntex < 16 * kTextonVariants)
+    ctx->tuner.settle(tx_key, kTextonVariants, 1);  // too few tiles to time
+  const bool tx_trial = !ctx->tuner.decided(tx_key);
+  bool tx_unused = false;
+  const int tx_var = tx_trial ? 1 : ctx->tuner.pick(tx_key, kTextonVariants, 1, 1, &tx_unused);
   auto pre_chain = [&]() -> cudaError_t {
     cudaError_t e;
 #define GK(x)                               \
@@ -1479,10 +1486,19 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     // (a) textons
     GK(launch_convert(b.packed, L.total_pix, b.grey, b.lab4, s));
     GK(cudaMemsetAsync(b.repair_count, 0, sizeof(int), s));
-    if (tx_trial) ctx->tuner.begin(tx_key, tx_var, s);
-    GK(launch_texton(b.patches, b.work_tex, (int)L.work_tex.size(), b.grey, b.lab4, b.repair, b.repair_count,
-                     repair_cap, s, tx_var));
-    if (tx_trial) ctx->tuner.end(s);
+    if (tx_trial) {
+      for (int v = 0; v < kTextonVariants; v++) {
+        const int t0 = ntex * v / kTextonVariants, t1 = ntex * (v + 1) / kTextonVariants;
+        ctx->tuner.begin(tx_key, v, s, (float)ntex / (float)(t1 - t0));
+        GK(launch_texton(b.patches, b.work_tex + t0, t1 - t0, b.grey, b.lab4, b.repair, b.repair_count, repair_cap,
+                         s, v));
+        ctx->tuner.end(s);
+      }
+      ctx->launches += kTextonVariants - 1;
+    } else {
+      GK(launch_texton(b.patches, b.work_tex, ntex, b.grey, b.lab4, b.repair, b.repair_count, repair_cap, s,
+                       tx_var));
+    }
     GK(launch_texton_repair(b.patches, b.grey, b.lab4, b.repair, b.repair_count, repair_cap, ctx->d_k32_ring,
                             ctx->d_ring_of, ctx->tab.n_rings, s));
     GK(stage_mark(ctx->ev[2], s));

@@ -60,13 +60,15 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float bhi, float bl
   hi = s;
   lo += e + blo;
 }
-__device__ __forceinline__ double ff_warp_reduce(float hi, float lo) {
+// float-float sum over the warp, in FP32 (every lane gets it); the FP64
+// pipe, about 1/64 of the FP32 rate here, is left to one conversion per CTA
+__device__ __forceinline__ float2 ff_warp_reduce(float hi, float lo) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const float h2 = __shfl_xor_sync(FULLM, hi, o), l2 = __shfl_xor_sync(FULLM, lo, o);
     ff_add(hi, lo, h2, l2);
   }
-  return (double)hi + (double)lo;
+  return make_float2(hi, lo);
 }
 
 // Last CTA of a patch: returns true in every thread of that CTA.
@@ -87,13 +89,13 @@ __device__ __forceinline__ bool last_cta(int* counter, int ntiles) {
 // per-warp partial sums (sred[warp][i], written by lane 0) -> one partial per
 // CTA in part[cta][i]
 constexpr int kRed = kMaxKrylov + 1;
-__device__ __forceinline__ void cta_partials(const double* sred, int nvals, double* part_row) {
+__device__ __forceinline__ void cta_partials(const float2* sred, int nvals, double* part_row) {
   __syncthreads();
   for (int i = threadIdx.x; i < nvals; i += blockDim.x) {
-    double s = 0;
+    float hi = 0.f, lo = 0.f;
 #pragma unroll
-    for (int w = 0; w < kEigWarps; w++) s += sred[w * kRed + i];
-    part_row[i] = s;
+    for (int w = 0; w < kEigWarps; w++) ff_add(hi, lo, sred[w * kRed + i].x, sred[w * kRed + i].y);
+    part_row[i] = (double)hi + (double)lo;
   }
 }
 // sum of one value over the CTAs of a patch, one warp, lanes strided
@@ -117,7 +119,7 @@ constexpr int kGrp = 4;
 // sred[warp][i]; v_j comes from registers (xj) when given
 __device__ __forceinline__ void basis_dots(const EigArgs& a, int j, const int (&qv)[kEigPix],
                                            const bool (&okv)[kEigPix], const float (&wv)[kEigPix],
-                                           const float* xj, double* sred, int warp, int lane) {
+                                           const float* xj, float2* sred, int warp, int lane) {
   for (int i0 = 0; i0 <= j; i0 += kGrp) {
     float vv[kGrp][kEigPix];
 #pragma unroll
@@ -138,7 +140,7 @@ __device__ __forceinline__ void basis_dots(const EigArgs& a, int j, const int (&
 #pragma unroll
     for (int u = 0; u < kGrp; u++) {
       if (i0 + u > j) break;
-      const double s = ff_warp_reduce(hi[u], lo[u]);
+      const float2 s = ff_warp_reduce(hi[u], lo[u]);
       if (lane == 0) sred[warp * kRed + i0 + u] = s;
     }
   }
@@ -153,7 +155,10 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_spmv(EigArgs a, int j, cons
   __shared__ int off[kUpper];
   if (threadIdx.x < kUpper) off[threadIdx.x] = c_up_dy[threadIdx.x] * P.W + c_up_dx[threadIdx.x];
   __syncthreads();
-  const float inv = use_beta ? (float)(1.0 / sqrt(a.beta2[t.patch])) : 1.f;
+  __shared__ float inv_s;
+  if (threadIdx.x == 0) inv_s = use_beta ? (float)(1.0 / sqrt(a.beta2[t.patch])) : 1.f;
+  __syncthreads();
+  const float inv = inv_s;
   const long long base = P.vec;
   // this thread's pixels; a pixel past the tile reads the tile's first one
   // (in bounds) and its results are dropped
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_spmv(EigArgs a, int j, cons
     dst[qv[r]] = wv[r];
   }
   // h_i = v_i . w for i <= j
-  __shared__ double sred[kEigWarps * kRed];
+  __shared__ float2 sred[kEigWarps * kRed];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   basis_dots(a, j, qv, okv, wv, xv, sred, warp, lane);
   cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
@@ -279,7 +284,7 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int 
 #pragma unroll
   for (int r = 0; r < kEigPix; r++)
     if (okv[r]) w[qv[r]] = wv[r];
-  __shared__ double sred[kEigWarps * kRed];
+  __shared__ float2 sred[kEigWarps * kRed];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (mode == 1) {
     basis_dots(a, j, qv, okv, wv, nullptr, sred, warp, lane);
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int 
 #pragma unroll
     for (int r = 0; r < kEigPix; r++)
       if (okv[r]) ff_add_prod(hi, lo, wv[r], wv[r]);
-    const double s = ff_warp_reduce(hi, lo);
+    const float2 s = ff_warp_reduce(hi, lo);
     if (lane == 0) sred[warp * kRed] = s;
     cta_partials(sred, 1, a.part + (long long)blockIdx.x * a.mp1);
   }
@@ -393,8 +398,8 @@ __global__ void __launch_bounds__(kEigThreads) ks_init(EigArgs a, float* __restr
     w[P.vec + p] = v;
     ff_add_prod(hi, lo, v, v);
   }
-  __shared__ double sred[kEigWarps * kRed];
-  const double s = ff_warp_reduce(hi, lo);
+  __shared__ float2 sred[kEigWarps * kRed];
+  const float2 s = ff_warp_reduce(hi, lo);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) sred[warp * kRed] = s;
   cta_partials(sred, 1, a.part + (long long)blockIdx.x * a.mp1);
