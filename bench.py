@@ -87,41 +87,51 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(img, cb, boxes, seconds=20.0):
+def cpu_baseline(img, cb, boxes, seconds=20.0, start=0):
     """Oracle (FP64 restatement of the reference CPU path) on whole patches of
-    the workload until about `seconds` of CPU work; Mpix/s over their
-    non-halo pixels."""
+    the workload, from patch `start` round the 16, until about `seconds` of
+    CPU work; Mpix/s over their non-halo pixels."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     done_px, t0, n = 0, time.time(), 0
-    for (y0, x0, h, w, iy, ix, ih, iw) in boxes:
+    for k in range(len(boxes)):
+        (y0, x0, h, w, iy, ix, ih, iw) = boxes[(start + k) % len(boxes)]
         po.globalpb(np.ascontiguousarray(img[y0:y0 + h, x0:x0 + w]), cb, po.params(threads=0))
         done_px += ih * iw
         n += 1
         if time.time() - t0 > seconds:
             break
     dt = time.time() - t0
-    return {"value": done_px / dt / 1e6, "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d of 16 patches of the workload, whole oracle pipeline (FP64)" % n}
+    return {"value": done_px / dt / 1e6, "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port", "patches": n,
+            "sample": "%d of 16 patches of the workload from patch %d, whole oracle pipeline (FP64)" % (n, start)}
 
 
 def run_reference(args):
+    """Each step times whole patches of the workload for about 10 s, each step
+    starting where the previous one stopped, so that the steps together go
+    round all 16 patches; Mpix/s is total non-halo pixels over total time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     img, cb, boxes, _ = make_workload()
-    per = []
+    px, sec, at, covered = 0.0, 0.0, 0, set()
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(img, cb, boxes, seconds=10.0 if i >= args.warmup else 1.0)
+        t0 = time.time()
+        r = cpu_baseline(img, cb, boxes, seconds=10.0 if i >= args.warmup else 1.0, start=at)
+        dt = time.time() - t0
         if i >= args.warmup:
-            per.append(r)
-    v = float(np.mean([r["value"] for r in per]))
+            px += r["value"] * dt * 1e6
+            sec += dt
+            covered.update((at + k) % len(boxes) for k in range(r["patches"]))
+        at = (at + r["patches"]) % len(boxes)
+    v = px / sec / 1e6
+    sample = ("per step about 10 s of whole patches, consecutive steps continuing round the 16 patches; "
+              "%d of the 16 timed over the %d steps" % (len(covered), args.steps))
     out = {"metric": METRIC, "value": v, "unit": "Mpix/s", "impl": "reference", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": WORKLOAD},
-           "cpu_baseline": {"value": v, "unit": "Mpix/s", "cores": per[0]["cores"], "kind": "port",
-                            "sample": per[0]["sample"] + " per step"},
+           "cpu_baseline": {"value": v, "unit": "Mpix/s", "cores": os.cpu_count(), "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
