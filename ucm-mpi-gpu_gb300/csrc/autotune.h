@@ -41,10 +41,8 @@ class Autotuner {
     for (cudaEvent_t e : free_) cudaEventDestroy(e);
   }
 
-  // The variant to launch for `key`, and whether this launch is a timed trial.
-  int pick(const std::string& key, int nvar, int reps, int fallback, bool* trial) {
-    *trial = false;
-    if (!enabled || nvar <= 1) return fallback;
+  // The entry of `key`, created with nvar variants and reps timings each.
+  Entry& entry(const std::string& key, int nvar, int reps) {
     Entry& e = tab_[key];
     if (e.nvar == 0) {
       e.nvar = nvar;
@@ -52,6 +50,14 @@ class Autotuner {
       e.ms.assign(nvar, {});
       e.issued.assign(nvar, 0);
     }
+    return e;
+  }
+
+  // The variant to launch for `key`, and whether this launch is a timed trial.
+  int pick(const std::string& key, int nvar, int reps, int fallback, bool* trial) {
+    *trial = false;
+    if (!enabled || nvar <= 1) return fallback;
+    Entry& e = entry(key, nvar, reps);
     if (e.chosen >= 0) return e.chosen;
     int v = 0;
     for (int i = 1; i < nvar; i++)
@@ -77,12 +83,7 @@ class Autotuner {
   }
   // registers a key and decides it at once (no trials worth timing)
   void settle(const std::string& key, int nvar, int v) {
-    Entry& e = tab_[key];
-    if (e.nvar == 0) {
-      e.nvar = nvar;
-      e.ms.assign(nvar, {});
-      e.issued.assign(nvar, 0);
-    }
+    Entry& e = entry(key, nvar, 1);
     if (e.chosen < 0) e.chosen = v;
   }
   void end(cudaStream_t s) {
@@ -94,7 +95,10 @@ class Autotuner {
   void collect() {
     for (auto& p : pend_) {
       float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) tab_[p.key].ms[p.v].push_back(ms * p.scale);
+      auto it = tab_.find(p.key);
+      if (it != tab_.end() && p.v >= 0 && p.v < (int)it->second.ms.size() &&
+          cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+        it->second.ms[p.v].push_back(ms * p.scale);
       free_.push_back(p.a);
       free_.push_back(p.b);
     }

@@ -1475,6 +1475,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
   if (ctx->tuner.enabled && !ctx->tuner.decided(tx_key) && ntex < 16 * kTextonVariants)
     ctx->tuner.settle(tx_key, kTextonVariants, 1);  // too few tiles to time
   const bool tx_trial = !ctx->tuner.decided(tx_key);
+  if (tx_trial) ctx->tuner.entry(tx_key, kTextonVariants, 1);
   bool tx_unused = false;
   const int tx_var = tx_trial ? 1 : ctx->tuner.pick(tx_key, kTextonVariants, 1, 1, &tx_unused);
   auto pre_chain = [&]() -> cudaError_t {
