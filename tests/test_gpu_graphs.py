@@ -34,6 +34,7 @@ def test_graph_replays_match_direct_launches(mode):
     cb, patches = _batch()
     direct = _env_context(cb, mode, "GPB_NO_GRAPHS")
     want = direct.compute_batch(patches)
+    direct.compute_batch(patches)  # the first call also runs the autotuner's trials
     assert direct.stats()["graph_replays"] == 0
     launches = direct.stats()["gpu_launches"]
     direct.close()
@@ -43,7 +44,8 @@ def test_graph_replays_match_direct_launches(mode):
         st = ctx.stats()
         for (nm_a, or_a), (nm_b, or_b) in zip(want, got):
             assert np.array_equal(nm_a, nm_b) and np.array_equal(or_a, or_b), call
-        assert st["gpu_launches"] == launches, call
+        if call:
+            assert st["gpu_launches"] == launches, call
     assert st["graph_replays"] > 0
     # another layout on the same context: its own graphs, the same bits
     sub = patches[1:3]

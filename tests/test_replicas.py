@@ -69,3 +69,46 @@ def test_gather_two_gloo_ranks():
     assert all(p.exitcode == 0 for p in procs)
     res = dict(q.get(timeout=10) for _ in range(2))
     assert res["ok"] > 0 and res["rank1"] > 0 and res["ok"] + res["rank1"] == 64
+
+
+def _fixture():
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "replica_costs.npz"))
+    return d["pixels"].astype(float), d["regions"].astype(float), d["ms"].astype(float), d["group"]
+
+
+def _ranks(x):
+    return np.argsort(np.argsort(x)).astype(float)
+
+
+def test_cost_model_ranks_measured_costs():
+    """The predicted cost ranks the measured solve times of 115 patches
+    (solved one at a time on a GB300) at least as well as the pixel count."""
+    from gpb import replicas
+    px, reg, ms, _ = _fixture()
+    model = px ** replicas.COST_EXP_PIXELS * (reg + 1) ** replicas.COST_EXP_REGIONS
+    rho = lambda a, b: np.corrcoef(_ranks(a), _ranks(b))[0, 1]
+    assert rho(model, ms) >= 0.9
+    assert rho(model, ms) >= rho(px, ms)
+
+
+def test_cost_split_balances_the_uneven_workload():
+    """On the 64 uneven patches, 8 ranks split by predicted cost carry a
+    smaller largest share of the measured time than a split by pixels."""
+    from gpb import replicas
+    px, reg, ms, group = _fixture()
+    m = group == 0
+    model = px[m] ** replicas.COST_EXP_PIXELS * (reg[m] + 1) ** replicas.COST_EXP_REGIONS
+    sizes = [(int(p), 1) for p in px[m]]
+
+    def worst(costs):
+        loads = [ms[m][s].sum() for s in replicas.partition(sizes, 8, costs)]
+        return max(loads) / np.mean(loads)
+    assert worst(list(model)) < worst(None)
+
+
+def test_predicted_cost_of_an_image():
+    from gpb import replicas, synth
+    a = synth.voronoi_image(96, 96, 4, 4.0, 1)
+    b = synth.voronoi_image(96, 96, 60, 4.0, 1)
+    assert replicas.regions(b) > replicas.regions(a)
+    assert replicas.predicted_cost(b) > replicas.predicted_cost(a)

@@ -194,6 +194,8 @@ struct gpb_ctx {
   bool use_graphs = true;
   // kernel variants chosen per shape bucket (autotune.h)
   Autotuner tuner;
+  // the Lab bins of every colour (k_lab_table), built at the first batch
+  uint32_t* d_lab_lut = nullptr;
   // the learned warm start's network (k_learned.cu), and the device staging
   // of a training minibatch
   std::unique_ptr<LearnedNet> net;
@@ -518,6 +520,7 @@ extern "C" void gpb_destroy(gpb_ctx* ctx) {
   drop_graphs(ctx);
   ctx->net.reset();
   if (ctx->d_tr) cudaFree(ctx->d_tr);
+  if (ctx->d_lab_lut) cudaFree(ctx->d_lab_lut);
   {
     ConstBank& bk = bank_of(ctx->device);
     std::lock_guard<std::mutex> lk(bk.mu);
@@ -1459,6 +1462,10 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
                          cudaMemcpyDeviceToDevice, s));
     }
   }
+  if (!ctx->d_lab_lut) {  // once per context; the gamma table it reads is constant
+    CK(cudaMalloc(&ctx->d_lab_lut, sizeof(uint32_t) << 24));
+    CK(launch_lab_table(ctx->d_lab_lut, s));
+  }
   CK(cudaEventRecord(ctx->ev[1], s));
   // (a)-(c): textons, local cues, NMS, buildW and the operator rows, one
   // fixed chain per batch layout
@@ -1485,7 +1492,7 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
     if ((e = (x)) != cudaSuccess) return e; \
   } while (0)
     // (a) textons
-    GK(launch_convert(b.packed, L.total_pix, b.grey, b.lab4, s));
+    GK(launch_convert_lut(b.packed, L.total_pix, ctx->d_lab_lut, b.grey, b.lab4, s));
     GK(cudaMemsetAsync(b.repair_count, 0, sizeof(int), s));
     if (tx_trial) {
       for (int v = 0; v < kTextonVariants; v++) {
@@ -1529,7 +1536,8 @@ static gpb_status run_batch(gpb_ctx* ctx, size_t n, const uint32_t* ws, const ui
                     repair_cap, ctx->tab.n_rings, blockm, ctx->prm.keep_intermediates, tx_var) +
                    gkey("", b.packed, b.grey, b.lab4, b.repair, b.repair_count, b.patches, b.work_tex, b.work_cue,
                         b.work16, b.nbins, b.mpbo, b.go, b.raw, b.counts, b.mpb, b.wup, b.deg, b.aup, b.adiag,
-                        b.dis, b.wfull, b.afull, b.berr, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of),
+                        b.dis, b.wfull, b.afull, b.berr, ctx->d_ic, ctx->d_k32_ring, ctx->d_ring_of,
+                        ctx->d_lab_lut),
                pre_chain, !tx_trial));
   // (d) eigensolver
   gpb_status es;

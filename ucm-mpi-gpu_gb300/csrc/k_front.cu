@@ -82,14 +82,8 @@ __device__ __forceinline__ int quant25(double v, int nbins) {
   return q == nbins ? nbins - 1 : q;
 }
 
-__global__ void __launch_bounds__(256) k_convert(const uint32_t* __restrict__ packed, long long n,
-                                                 uint8_t* __restrict__ grey,
-                                                 uint32_t* __restrict__ lab4) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t px = packed[i];
-  const int B = (px >> 16) & 255, G = (px >> 8) & 255, R = px & 255;
-  grey[i] = (uint8_t)((R * 4899 + G * 9617 + B * 1868 + (1 << 13)) >> 14);
+// Lab bins (L | a << 8 | b << 16) of one BGR colour
+__device__ __forceinline__ uint32_t lab_bins_of(int R, int G, int B) {
   // D1 fixed: r = R, b = B
   const double r = c_gamma[R], g = c_gamma[G], b = c_gamma[B];
   const double X = __dadd_rn(__dadd_rn(__dmul_rn(0.412453, r), __dmul_rn(0.357580, g)), __dmul_rn(0.180423, b));
@@ -106,7 +100,40 @@ __global__ void __launch_bounds__(256) k_convert(const uint32_t* __restrict__ pa
   const int qL = quant25(__ddiv_rn(L, 100.0), 25);
   const int qa = quant25(__ddiv_rn(__dsub_rn(A, -73.0), 168.0), 25);
   const int qb = quant25(__ddiv_rn(__dsub_rn(Bb, -73.0), 168.0), 25);
-  lab4[i] = (uint32_t)qL | ((uint32_t)qa << 8) | ((uint32_t)qb << 16);
+  return (uint32_t)qL | ((uint32_t)qa << 8) | ((uint32_t)qb << 16);
+}
+
+__device__ __forceinline__ uint8_t grey_of(int R, int G, int B) {
+  return (uint8_t)((R * 4899 + G * 9617 + B * 1868 + (1 << 13)) >> 14);
+}
+
+__global__ void __launch_bounds__(256) k_convert(const uint32_t* __restrict__ packed, long long n,
+                                                 uint8_t* __restrict__ grey,
+                                                 uint32_t* __restrict__ lab4) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t px = packed[i];
+  const int B = (px >> 16) & 255, G = (px >> 8) & 255, R = px & 255;
+  grey[i] = grey_of(R, G, B);
+  lab4[i] = lab_bins_of(R, G, B);
+}
+
+// The Lab bins of all 2^24 colours, indexed by the packed value B<<16|G<<8|R:
+// the pipeline's convert step then gathers from this table (FP64 cube roots
+// run at a small fraction of the FP32 rate on this part).
+__global__ void __launch_bounds__(256) k_lab_table(uint32_t* __restrict__ table) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < (1u << 24); c += gridDim.x * blockDim.x)
+    table[c] = lab_bins_of(c & 255, (c >> 8) & 255, c >> 16);
+}
+
+__global__ void __launch_bounds__(256) k_convert_lut(const uint32_t* __restrict__ packed, long long n,
+                                                     const uint32_t* __restrict__ table,
+                                                     uint8_t* __restrict__ grey, uint32_t* __restrict__ lab4) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t px = packed[i];
+  grey[i] = grey_of(px & 255, (px >> 8) & 255, (px >> 16) & 255);
+  lab4[i] = __ldg(table + (px & 0xffffffu));
 }
 
 // ----------------------------------------------------------------- texton
@@ -280,6 +307,16 @@ cudaError_t launch_convert(const uint32_t* packed, long long n, uint8_t* grey, u
                            cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   k_convert<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(packed, n, grey, lab4);
+  return cudaGetLastError();
+}
+cudaError_t launch_lab_table(uint32_t* table, cudaStream_t s) {
+  k_lab_table<<<4096, 256, 0, s>>>(table);
+  return cudaGetLastError();
+}
+cudaError_t launch_convert_lut(const uint32_t* packed, long long n, const uint32_t* table, uint8_t* grey,
+                               uint32_t* lab4, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  k_convert_lut<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(packed, n, table, grey, lab4);
   return cudaGetLastError();
 }
 

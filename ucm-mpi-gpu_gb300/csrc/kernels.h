@@ -13,6 +13,11 @@ void upload_front(const HostTables& t, cudaStream_t s);
 void upload_codebook(const float* cb, int K, cudaStream_t s);
 cudaError_t launch_convert(const uint32_t* packed, long long n, uint8_t* grey, uint32_t* lab4,
                            cudaStream_t s);
+// the Lab bins of all 2^24 colours (a 64 MB table), and the convert step as
+// a gather from it
+cudaError_t launch_lab_table(uint32_t* table, cudaStream_t s);
+cudaError_t launch_convert_lut(const uint32_t* packed, long long n, const uint32_t* table, uint8_t* grey,
+                               uint32_t* lab4, cudaStream_t s);
 // variant 0, 1, 2: 32, 64 or 128 threads per 16 x 16 tile (identical labels)
 constexpr int kTextonVariants = 3;
 cudaError_t launch_texton(const PatchDev* patches, const int4* work, int nwork, const uint8_t* grey,
