@@ -99,10 +99,11 @@ def init_params(seed=0):
     return p
 
 
-def evaluate(weights, n=32, size=512, seed=77, batch=8, modes=None):
-    """Per eigensolver mode: eigensolver ms per batch (device events), matvecs,
+def evaluate(weights, n=32, size=512, seed=77, batch=8, modes=None, tol=None, gap_frac=None):
+    """Per eigensolver mode: eigensolver ms per patch (device events), matvecs,
     largest residual, over held-out patches; the learned and cold-start
-    block solvers' gPb planes compared."""
+    block solvers' gPb planes compared.  tol / gap_frac override eig_tol /
+    eig_gap_frac (gap_frac 0: the residual criterion alone)."""
     import torch
     import gpb
     imgs = images(n, size, 1000 + seed)
@@ -111,8 +112,13 @@ def evaluate(weights, n=32, size=512, seed=77, batch=8, modes=None):
     modes = modes or {"learned": gpb.EIG_LEARNED, "cold_block": gpb.EIG_BLOCK, "coarse_warm": gpb.EIG_WARM,
                       "plain_lanczos": gpb.EIG_LANCZOS}
     res, planes = {}, {}
+    over = {}
+    if tol is not None:
+        over["eig_tol"] = tol
+    if gap_frac is not None:
+        over["eig_gap_frac"] = gap_frac
     for name, mode in modes.items():
-        ctx = gpb.Context(cb, eig_mode=mode)
+        ctx = gpb.Context(cb, eig_mode=mode, **over)
         if mode == gpb.EIG_LEARNED:
             ctx.learned_set(weights)
         ctx.compute_batch(packed[:batch])  # layout, autotuning, graphs
@@ -145,6 +151,8 @@ def main():
     ap.add_argument("--eval", default=None)
     ap.add_argument("--n", type=int, default=32)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--tol", type=float, default=None)
+    ap.add_argument("--gap-frac", type=float, default=None)
     args = ap.parse_args()
     rep = {}
     if args.train:
@@ -153,7 +161,7 @@ def main():
         rep["train"] = {"patches": args.train, "size": args.size, "epochs": args.epochs, "batch": args.batch,
                         "lr": args.lr, "loss_per_epoch": hist.tolist(), **t}
     if args.eval:
-        rep["eval"] = evaluate(np.load(args.eval), n=args.n, size=512)
+        rep["eval"] = evaluate(np.load(args.eval), n=args.n, size=512, tol=args.tol, gap_frac=args.gap_frac)
         print(json.dumps(rep["eval"]))
     if args.report:
         with open(args.report, "w") as f:
