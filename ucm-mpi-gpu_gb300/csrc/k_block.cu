@@ -428,44 +428,69 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
   }
 }
 
+// A ROWS x 16 tile's pixel-major rows (NC floats each), staged in shared
+// memory by pixel 16 * ty + tx, out to their places: a tile row's pixels are
+// adjacent in the layout, so each tile row leaves as one contiguous run of
+// 16-byte stores.  (A thread writing its own row would give each warp store
+// 32 scattered 16-byte pieces.)  Row strides of 21 and 13 float4 put the 8
+// threads of a staging store's phase in distinct banks.
+template <int NC, int ROWS>
+__device__ __forceinline__ void tile_rows_out(const float4* __restrict__ rows, float* __restrict__ dst, long long vec,
+                                              int W, int H, int y0, int x0) {
+  constexpr int Q = NC / 4;
+  const int ny = min(ROWS, H - y0), nx = min(16, W - x0);
+  for (int i = threadIdx.x; i < ny * 16 * Q; i += blockDim.x) {
+    const int r = i / (16 * Q), j = i % (16 * Q);
+    if (j < nx * Q) ((float4*)(dst + (vec + (long long)(y0 + r) * W + x0) * NC))[j] = rows[r * 16 * Q + j];
+  }
+}
+
 // pixel-major full stencil rows of the fine operator from its symmetric
 // storage: row p holds A(p, p + off_e) for the 81 offsets e in scanline
 // order (0 where the neighbour is outside the patch), then 3 zeros
-__global__ void __launch_bounds__(256) cf_full(const PatchDev* __restrict__ patches, const int4* __restrict__ work,
-                                               const float* __restrict__ a_up, const float* __restrict__ a_diag,
-                                               long long lvec, float* __restrict__ afull) {
-  // one thread per pixel of the 16 x 16 tile: the plane reads are coalesced
-  // across the warp, the row goes out as 21 16-byte stores
-  const int4 w = work[blockIdx.x];
-  const PatchDev P = patches[w.x];
+constexpr int kFullRows = 8;  // tile rows per CTA: half of a 16 x 16 work tile
+__global__ void __launch_bounds__(kFullRows * 16) cf_full(const PatchDev* __restrict__ patches,
+                                                          const int4* __restrict__ work,
+                                                          const float* __restrict__ a_up,
+                                                          const float* __restrict__ a_diag, long long lvec,
+                                                          float* __restrict__ afull) {
+  // one thread per pixel of a half tile (43 KB of staging, so several CTAs
+  // share an SM): the plane reads are coalesced across the warp; the rows go
+  // out through shared memory
   constexpr int NC = DiskStencil::NC, ctr = kStencilN / 2;
-  const int y = w.y + threadIdx.x / 16, x = w.z + threadIdx.x % 16;
-  if (y >= P.H || x >= P.W) return;
-  const long long p = P.vec + (long long)y * P.W + x;
-  float4* row = (float4*)(afull + p * NC);
-#pragma unroll 1
-  for (int e4 = 0; e4 < NC / 4; e4++) {
-    float v[4];
+  __shared__ float4 rows[kFullRows * 16 * (NC / 4)];
+  const int4 w = work[blockIdx.x >> 1];
+  const PatchDev P = patches[w.x];
+  const int y0 = w.y + (blockIdx.x & 1) * kFullRows;
+  const int y = y0 + threadIdx.x / 16, x = w.z + threadIdx.x % 16;
+  if (y < P.H && x < P.W) {
+    const long long p = P.vec + (long long)y * P.W + x;
+#pragma unroll 3
+    for (int e4 = 0; e4 < NC / 4; e4++) {
+      float v[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int e = 4 * e4 + j;
-      v[j] = 0.f;
-      if (e >= kStencilN) continue;
-      if (e == ctr) {
-        v[j] = a_diag[p];
-        continue;
+      for (int j = 0; j < 4; j++) {
+        const int e = 4 * e4 + j;
+        v[j] = 0.f;
+        if (e >= kStencilN) continue;
+        if (e == ctr) {
+          v[j] = a_diag[p];
+          continue;
+        }
+        // upper offsets are c_bup[e - 41]; the disk is point-symmetric, so
+        // lower offset e mirrors upper offset 80 - e
+        const int k = e > ctr ? e - ctr - 1 : kStencilN - 1 - e - ctr - 1;
+        const int dy = e > ctr ? c_bup_dy[k] : -c_bup_dy[k];
+        const int dx = e > ctr ? c_bup_dx[k] : -c_bup_dx[k];
+        const int yy = y + dy, xx = x + dx;
+        if (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W)
+          v[j] = e > ctr ? a_up[(long long)k * lvec + p] : a_up[(long long)k * lvec + p + (long long)dy * P.W + dx];
       }
-      // upper offsets are c_bup[e - 41]; the disk is point-symmetric, so
-      // lower offset e mirrors upper offset 80 - e
-      const int k = e > ctr ? e - ctr - 1 : kStencilN - 1 - e - ctr - 1;
-      const int dy = e > ctr ? c_bup_dy[k] : -c_bup_dy[k];
-      const int dx = e > ctr ? c_bup_dx[k] : -c_bup_dx[k];
-      const int yy = y + dy, xx = x + dx;
-      if (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W)
-        v[j] = e > ctr ? a_up[(long long)k * lvec + p] : a_up[(long long)k * lvec + p + (long long)dy * P.W + dx];
+      rows[threadIdx.x * (NC / 4) + e4] = make_float4(v[0], v[1], v[2], v[3]);
     }
-    row[e4] = make_float4(v[0], v[1], v[2], v[3]);
   }
+  __syncthreads();
+  tile_rows_out<NC, kFullRows>(rows, afull, P.vec, P.W, P.H, y0, w.z);
 }
 
 // ------------------------------------------------------------------ Gram
@@ -704,61 +729,105 @@ __global__ void __launch_bounds__(256) cf_init(BlkArgs a, float* __restrict__ X)
 // p in P, q in Q, so (D_c - W_c) u = lambda D_c u is the projection of the
 // fine generalised problem onto block-constant vectors.  Fine radius 5 gives
 // coarse offsets up to 3: a full 7 x 7 stencil, stored per offset.
-__global__ void __launch_bounds__(256) cf_coarsen(CoarseArgs c) {
+// coarse degrees d_c(P) = the sum of the fine degrees of P's pixels (the
+// row sums of W_c, since W_c(P, Q) sums W over P x Q), and D_c^-1/2
+__global__ void __launch_bounds__(256) cf_coarse_deg(CoarseArgs c) {
   const int4 w = c.work[blockIdx.x];  // coarse (patch, Y0, X0)
   const PatchDev F = c.fine[w.x], C = c.coarse[w.x];
   const int Y = w.y + threadIdx.x / 16, X = w.z + threadIdx.x % 16;
   if (Y >= C.H || X >= C.W) return;
-  float acc[kCN];
-#pragma unroll
-  for (int k = 0; k < kCN; k++) acc[k] = 0.f;
   double deg = 0.0;
   for (int sy = 0; sy < 2; sy++)
     for (int sx = 0; sx < 2; sx++) {
       const int y = 2 * Y + sy, x = 2 * X + sx;
-      if (y >= F.H || x >= F.W) continue;
-      const long long p = F.vec + (long long)y * F.W + x;
-      acc[kCR * kCW + kCR] += 1.f;  // w_pp = 1
-      deg += c.deg[p];
-      for (int j = 0; j < kUpper; j++) {
-        const int dy = c_bup_dy[j], dx = c_bup_dx[j];
-        // upper neighbour q = p + (dy,dx) and lower neighbour q = p - (dy,dx)
-        for (int sgn = -1; sgn <= 1; sgn += 2) {
-          const int yy = y + sgn * dy, xx = x + sgn * dx;
-          if (yy < 0 || yy >= F.H || xx < 0 || xx >= F.W) continue;
-          const long long off = (long long)dy * F.W + dx;
-          const float wv = sgn > 0 ? c.wsym_up[(long long)j * c.lvec_f + p] : c.wsym_up[(long long)j * c.lvec_f + p - off];
-          const int dY = (yy >> 1) - Y, dX = (xx >> 1) - X;
-          acc[(dY + kCR) * kCW + (dX + kCR)] += wv;
-        }
-      }
+      if (y < F.H && x < F.W) deg += c.deg[F.vec + (long long)y * F.W + x];
     }
   const long long P = C.vec + (long long)Y * C.W + X;
-  constexpr int NC = SquareStencil::NC;
-#pragma unroll
-  for (int k = 0; k < NC; k++) c.wc[P * NC + k] = k < kCN ? acc[k] : 0.f;
   c.degc[P] = (float)deg;
   c.disc[P] = (float)(1.0 / sqrt(deg));
 }
 
-// A_c = I - D_c^-1/2 W_c D_c^-1/2 in place on wc
-__global__ void __launch_bounds__(256) cf_coarse_norm(CoarseArgs c) {
-  const int4 w = c.work[blockIdx.x];
-  const PatchDev C = c.coarse[w.x];
-  const int Y = w.y + threadIdx.x / 16, X = w.z + threadIdx.x % 16;
-  if (Y >= C.H || X >= C.W) return;
-  const long long P = C.vec + (long long)Y * C.W + X;
-  const float dp = c.disc[P];
-  constexpr int NC = SquareStencil::NC;
-  for (int k = 0; k < kCN; k++) {
-    const int dY = k / kCW - kCR, dX = k % kCW - kCR;
-    const int YY = Y + dY, XX = X + dX;
-    float v = 0.f;
-    if (YY >= 0 && YY < C.H && XX >= 0 && XX < C.W)
-      v = -c.wc[P * NC + k] * dp * c.disc[C.vec + (long long)YY * C.W + XX];
-    if (k == kCR * kCW + kCR) v += 1.f;
-    c.wc[P * NC + k] = v;
+// coarse stencil index of fine displacement (a, b) from sub-pixel (0, 0):
+// coarse offset (floor(a / 2), floor(b / 2)), a, b in [-5, 6]
+__host__ __device__ constexpr int cidx(int a, int b) {
+  return ((a + 8) / 2 - 4 + kCR) * kCW + (b + 8) / 2 - 4 + kCR;
+}
+static_assert(cidx(0, 0) == kCR * kCW + kCR && cidx(-5, -5) == 0 && cidx(6, 6) == kCN - 1, "coarse offsets");
+
+// upper offset j's displacement (the inverse of upper_k)
+__host__ __device__ constexpr int upper_dy_from(int j, int dy) {
+  return j < 2 * disk_half_width(dy) + 1 ? dy : upper_dy_from(j - 2 * disk_half_width(dy) - 1, dy + 1);
+}
+__host__ __device__ constexpr int upper_dy(int j) { return j < kStencilR ? 0 : upper_dy_from(j - kStencilR, 1); }
+__host__ __device__ constexpr int upper_dx(int j) {
+  return upper_dy(j) == 0 ? j + 1 : j - upper_k(upper_dy(j), 0);
+}
+static_assert(upper_dy(0) == 0 && upper_dx(0) == 1 && upper_dy(5) == 1 && upper_dx(5) == -4 &&
+                  upper_dy(kUpper - 1) == kStencilR && upper_dx(kUpper - 1) == 0 && upper_k(upper_dy(23), upper_dx(23)) == 23,
+              "upper offset inverse");
+
+// the terms of fine sub-pixel (SY, SX) of a coarse pixel: upper offset J's
+// lower neighbour q = p - (dy,dx) (its upper entry at q), then its upper
+// neighbour q = p + (dy,dx); each lands on a compile-time coarse offset
+template <int SY, int SX, int J>
+__device__ __forceinline__ void coarsen_terms(float (&acc)[kCN], const float* __restrict__ wsym, long long lvec,
+                                              long long p, int y, int x, int H, int W) {
+  if constexpr (J < kUpper) {
+    constexpr int dy = upper_dy(J), dx = upper_dx(J);
+    const float* plane = wsym + (long long)J * lvec;
+    if (y - dy >= 0 && x - dx >= 0 && x - dx < W) acc[cidx(SY - dy, SX - dx)] += plane[p - (dy * W + dx)];
+    if (y + dy < H && x + dx >= 0 && x + dx < W) acc[cidx(SY + dy, SX + dx)] += plane[p];
+    coarsen_terms<SY, SX, J + 1>(acc, wsym, lvec, p, y, x, H, W);
   }
+}
+template <int SY, int SX>
+__device__ __forceinline__ void coarsen_sub(float (&acc)[kCN], const CoarseArgs& c, const PatchDev& F, int Y, int X) {
+  const int y = 2 * Y + SY, x = 2 * X + SX;
+  if (y < F.H && x < F.W) {
+    acc[kCR * kCW + kCR] += 1.f;  // w_pp = 1
+    coarsen_terms<SY, SX, 0>(acc, c.wsym_up, c.lvec_f, F.vec + (long long)y * F.W + x, y, x, F.H, F.W);
+  }
+}
+
+// W_c row of one coarse pixel, then A_c = I - D_c^-1/2 W_c D_c^-1/2 on it.
+// The fine offsets, the two signs and the 2 x 2 sub-pixels are unrolled at
+// compile time, so every term's coarse offset -- floor((s + dy) / 2) for
+// sub-pixel s -- is a constant and the 49 sums stay in registers.  Terms
+// are added per sum in the order: sub-pixel, upper offset, lower before
+// upper neighbour.
+__global__ void __launch_bounds__(256) cf_coarsen(CoarseArgs c) {
+  extern __shared__ float4 rows[];  // [256][13]
+  const int4 w = c.work[blockIdx.x];
+  const PatchDev F = c.fine[w.x], C = c.coarse[w.x];
+  constexpr int NC = SquareStencil::NC;
+  const int Y = w.y + threadIdx.x / 16, X = w.z + threadIdx.x % 16;
+  if (Y < C.H && X < C.W) {
+    float acc[kCN];
+#pragma unroll
+    for (int k = 0; k < kCN; k++) acc[k] = 0.f;
+    coarsen_sub<0, 0>(acc, c, F, Y, X);
+    coarsen_sub<0, 1>(acc, c, F, Y, X);
+    coarsen_sub<1, 0>(acc, c, F, Y, X);
+    coarsen_sub<1, 1>(acc, c, F, Y, X);
+    const long long P = C.vec + (long long)Y * C.W + X;
+    const float dp = c.disc[P];
+    float v[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) {
+      v[k] = 0.f;
+      if (k >= kCN) continue;
+      const int dY = k / kCW - kCR, dX = k % kCW - kCR;
+      const int YY = Y + dY, XX = X + dX;
+      if (YY >= 0 && YY < C.H && XX >= 0 && XX < C.W)
+        v[k] = -acc[k] * dp * c.disc[C.vec + (long long)YY * C.W + XX];
+      if (k == kCR * kCW + kCR) v[k] += 1.f;
+    }
+#pragma unroll
+    for (int q = 0; q < NC / 4; q++)
+      rows[threadIdx.x * (NC / 4) + q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  }
+  __syncthreads();
+  tile_rows_out<NC, 16>(rows, c.wc, C.vec, C.W, C.H, w.y, w.z);
 }
 
 // fine start block from the coarse Ritz vectors: the coarse generalised
@@ -801,9 +870,15 @@ __global__ void __launch_bounds__(256) cf_prolong(CoarseArgs c, const float* __r
   }
 }
 
+constexpr int kCoarsenSmem = 256 * kCoarseNC * sizeof(float);
 cudaError_t cf_launch_coarsen(const CoarseArgs& c, int nwork_c, cudaStream_t s) {
-  cf_coarsen<<<nwork_c, 256, 0, s>>>(c);
-  cf_coarse_norm<<<nwork_c, 256, 0, s>>>(c);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(cf_coarsen, cudaFuncAttributeMaxDynamicSharedMemorySize, kCoarsenSmem);
+    attr = true;
+  }
+  cf_coarse_deg<<<nwork_c, 256, 0, s>>>(c);
+  cf_coarsen<<<nwork_c, 256, kCoarsenSmem, s>>>(c);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc, float* xf, cudaStream_t s) {
@@ -865,7 +940,7 @@ cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const 
 }
 cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwork, const float* a_up,
                            const float* a_diag, long long lvec, float* afull, cudaStream_t s) {
-  cf_full<<<nwork, 256, 0, s>>>(patches, work16, a_up, a_diag, lvec, afull);
+  cf_full<<<2 * nwork, kFullRows * 16, 0, s>>>(patches, work16, a_up, a_diag, lvec, afull);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,

@@ -89,7 +89,12 @@ __global__ void __launch_bounds__(256) k_buildw(const PatchDev* __restrict__ pat
   }
 }
 
-// degree d_p = sum of the 81 symmetric affinities (diagonal 1), D^-1/2
+// degree d_p = sum of the 81 symmetric affinities (diagonal 1), D^-1/2.
+// The sum is a float-float pair built by Fast2Sum (Dekker 1971; exact since
+// the running sum, at least the diagonal 1, is never below a term in [0, 1]),
+// so it holds the 81-term sum to about 2^-44 relative -- as close as an FP64
+// accumulation at GB300's low FP64 rate would, on the FP32 pipes.  The
+// unrolled offset loop issues the plane loads independently.
 __global__ void __launch_bounds__(256) k_degree(const PatchDev* __restrict__ patches,
                                                 const int4* __restrict__ work,
                                                 const float* __restrict__ wsym_up, float* __restrict__ deg,
@@ -100,22 +105,30 @@ __global__ void __launch_bounds__(256) k_degree(const PatchDev* __restrict__ pat
   const int y = w.y + threadIdx.x / 16, x = w.z + threadIdx.x % 16;
   if (y >= P.H || x >= P.W) return;
   const long long p = (long long)y * P.W + x;
-  double d = 1.0;
+  const float* wp = wsym_up + P.vec + p;
+  float hi = 1.f, lo = 0.f;
+#pragma unroll 8
   for (int j = 0; j < kUpper; j++) {
     const int k = kStencilN / 2 + 1 + j;
-    const long long off = (long long)c_sdy[k] * P.W + c_sdx[k];
-    const float up = wsym_up[(long long)j * lvec + P.vec + p];
-    const float lo = wsym_up[(long long)j * lvec + P.vec + p - off];  // zero in the pad
+    const int off = c_sdy[k] * P.W + c_sdx[k];
+    const float up = wp[(long long)j * lvec];
+    const float lw = wp[(long long)j * lvec - off];  // zero in the pad
     // the lower entry is valid only if the neighbour lies inside the patch
     const int yy = y - c_sdy[k], xx = x - c_sdx[k];
-    const float lov = (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W) ? lo : 0.f;
-    d += (double)up + (double)lov;
+    const float lov = (yy >= 0 && yy < P.H && xx >= 0 && xx < P.W) ? lw : 0.f;
+    float sum = __fadd_rn(hi, up);
+    lo = __fadd_rn(lo, __fsub_rn(up, __fsub_rn(sum, hi)));
+    hi = sum;
+    sum = __fadd_rn(hi, lov);
+    lo = __fadd_rn(lo, __fsub_rn(lov, __fsub_rn(sum, hi)));
+    hi = sum;
     if (wfull) {
       wfull[(P.pix + p) * kStencilN + k] = up;
       wfull[(P.pix + p) * kStencilN + (kStencilN - 1 - k)] = lov;
     }
   }
   if (wfull) wfull[(P.pix + p) * kStencilN + kStencilN / 2] = 1.f;
+  const double d = (double)hi + (double)lo;
   deg[P.vec + p] = (float)d;
   dis[P.vec + p] = (float)(1.0 / sqrt(d));
   a_diag[P.vec + p] = (float)((d - 1.0) / d);
