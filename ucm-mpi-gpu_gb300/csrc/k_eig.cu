@@ -12,14 +12,16 @@
 //             written on the fly, h = V^T w
 //   ks_orth   w -= V h, h2 = V^T w          (classical Gram-Schmidt, pass 1)
 //   ks_orth   w -= V h2, beta^2 = |w|^2     (pass 2)
-// Dot products are accumulated in compensated FP32 (float-float: exact
-// product error by FMA plus two-sum), about as accurate as FP64
-// accumulation, whose rate on this part is 1/64 of FP32; the per-CTA
-// partials are reduced in FP64 by the last CTA of each patch to finish
-// (threadfence + atomic counter), so no separate reduction launches.
+// Dot products are FMA chains over a thread's pixels, summed across the
+// warp and the CTA in float-float (a compensated FP32 pair; FP64 runs at
+// 1/64 of the FP32 rate on this part); the first CGS pass's projection V h,
+// whose subtraction cancels most of w on a converging step, is formed
+// float-float with exact products.  The per-CTA partials are reduced in FP64
+// by the last CTA of each patch to finish (threadfence + atomic counter), so
+// no separate reduction launches.
 // The projected matrix T lives in device memory; at the end of a restart
 // cycle the host solves it (eig_host.cpp) and ks_restart assembles the kept
-// Ritz vectors in place with compensated sums.
+// Ritz vectors.
 #include <stdint.h>
 
 #include "gpb_internal.h"
@@ -113,13 +115,41 @@ __device__ __forceinline__ double patch_sum(const double* part, int tb, int tc, 
 // same order (offsets ascending, basis vectors ascending, pixels ascending).
 // Pixels are addressed by 32-bit offsets into the vector layout, which the
 // host keeps below 2^31 entries.
-constexpr int kGrp = 4;
+constexpr int kGrp = 8;
 
-// h_i = v_i . w for i = 0..j over this thread's pixels, reduced per warp into
-// sred[warp][i]; v_j comes from registers (xj) when given
+// Sums kGrp = 8 float-float values over the warp at once.  Each of the first
+// three xor rounds halves the values a lane carries (it keeps the half its
+// lane bit selects and sends the other), the last two are plain: 18
+// exchanges of a (hi, lo) pair and 9 float-float additions for the 8 values
+// instead of 80 and 40.  Lane l ends with the total of value l >> 2.
+__device__ __forceinline__ float2 ff_warp_reduce8(float (&hi)[kGrp], float (&lo)[kGrp], int lane) {
+#pragma unroll
+  for (int half = 4, o = 16; half >= 1; half >>= 1, o >>= 1) {
+    const bool b = lane & o;
+#pragma unroll
+    for (int i = 0; i < half; i++) {
+      const float kh = b ? hi[i + half] : hi[i], kl = b ? lo[i + half] : lo[i];
+      const float gh = b ? hi[i] : hi[i + half], gl = b ? lo[i] : lo[i + half];
+      hi[i] = kh;
+      lo[i] = kl;
+      ff_add(hi[i], lo[i], __shfl_xor_sync(FULLM, gh, o), __shfl_xor_sync(FULLM, gl, o));
+    }
+  }
+#pragma unroll
+  for (int o = 2; o >= 1; o >>= 1) ff_add(hi[0], lo[0], __shfl_xor_sync(FULLM, hi[0], o), __shfl_xor_sync(FULLM, lo[0], o));
+  return make_float2(hi[0], lo[0]);
+}
+
+// h_i = v_i . w for i = 0..j over this thread's pixels (w is 0 at a pixel
+// past the tile), reduced per warp into sred[warp][i]; v_j comes from
+// registers (xj) when given.  A plain FMA chain over the thread's eight
+// pixels, then float-float across threads: the error of a dot is a few
+// units of rounding times |w| (Cauchy-Schwarz over the thread partials),
+// which after the second pass leaves the basis orthogonal to ~1e-7 --
+// two orders below what the Ritz residuals need.
 __device__ __forceinline__ void basis_dots(const EigArgs& a, int j, const int (&qv)[kEigPix],
-                                           const bool (&okv)[kEigPix], const float (&wv)[kEigPix],
-                                           const float* xj, float2* sred, int warp, int lane) {
+                                           const float (&wv)[kEigPix], const float* xj, float2* sred, int warp,
+                                           int lane) {
   for (int i0 = 0; i0 <= j; i0 += kGrp) {
     float vv[kGrp][kEigPix];
 #pragma unroll
@@ -134,15 +164,11 @@ __device__ __forceinline__ void basis_dots(const EigArgs& a, int j, const int (&
     for (int u = 0; u < kGrp; u++) {
       hi[u] = lo[u] = 0.f;
 #pragma unroll
-      for (int r = 0; r < kEigPix; r++)
-        if (okv[r]) ff_add_prod(hi[u], lo[u], vv[u][r], wv[r]);
+      for (int r = 0; r < kEigPix; r++) hi[u] = fmaf(vv[u][r], wv[r], hi[u]);
     }
-#pragma unroll
-    for (int u = 0; u < kGrp; u++) {
-      if (i0 + u > j) break;
-      const float2 s = ff_warp_reduce(hi[u], lo[u]);
-      if (lane == 0) sred[warp * kRed + i0 + u] = s;
-    }
+    const float2 sum = ff_warp_reduce8(hi, lo, lane);
+    const int i = i0 + (lane >> 2);
+    if ((lane & 3) == 0 && i <= j) sred[warp * kRed + i] = sum;
   }
 }
 
@@ -208,7 +234,9 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_spmv(EigArgs a, int j, cons
   // h_i = v_i . w for i <= j
   __shared__ float2 sred[kEigWarps * kRed];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  basis_dots(a, j, qv, okv, wv, xv, sred, warp, lane);
+  // the second pass measures what these dots missed (h2 = V^T (w - V h)),
+  // and T takes h + h2
+  basis_dots(a, j, qv, wv, xv, sred, warp, lane);
   cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
   if (last_cta(a.counter + t.patch, a.tile_count[t.patch])) {
     const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
@@ -225,8 +253,12 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_spmv(EigArgs a, int j, cons
 }
 
 // --------------------------------------------------------------- CGS pass
-// mode 1: w -= V h, then h2 = V^T w;  mode 2: w -= V h2, then |w|^2
-__global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int mode, float* __restrict__ w) {
+// MODE 1: w -= V h, then h2 = V^T w;  MODE 2: w -= V h2, then |w|^2.
+// Pass 1 subtracts a projection of about |w|'s size (the cancellation of a
+// converging step), so V h is formed in float-float and subtracted exactly;
+// pass 2's V h2 is of rounding-error size and an FMA chain holds it.
+template <int MODE>
+__global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, float* __restrict__ w) {
   const EigTile t = a.tiles[blockIdx.x];
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
@@ -266,28 +298,34 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int 
       const float h = hs[i0 + u], h2 = hl[i0 + u];
 #pragma unroll
       for (int r = 0; r < kEigPix; r++) {
-        if (okv[r]) {
+        if constexpr (MODE == 1) {
           ff_add_prod(sh[r], sl[r], h, vv[u][r]);
           sl[r] = fmaf(h2, vv[u][r], sl[r]);
+        } else {
+          sh[r] = fmaf(h, vv[u][r], sh[r]);
         }
       }
     }
   }
 #pragma unroll
   for (int r = 0; r < kEigPix; r++) {
-    // w - (sh + sl) with the subtraction of sh exact (two-difference)
-    const float d = wv[r] - sh[r];
-    const float z = d - wv[r];
-    const float e = (wv[r] - (d - z)) - (sh[r] + z);
-    wv[r] = okv[r] ? d + (e - sl[r]) : 0.f;
+    if constexpr (MODE == 1) {
+      // w - (sh + sl) with the subtraction of sh exact (two-difference)
+      const float d = wv[r] - sh[r];
+      const float z = d - wv[r];
+      const float e = (wv[r] - (d - z)) - (sh[r] + z);
+      wv[r] = okv[r] ? d + (e - sl[r]) : 0.f;
+    } else {
+      wv[r] = okv[r] ? wv[r] - sh[r] : 0.f;
+    }
   }
 #pragma unroll
   for (int r = 0; r < kEigPix; r++)
     if (okv[r]) w[qv[r]] = wv[r];
   __shared__ float2 sred[kEigWarps * kRed];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (mode == 1) {
-    basis_dots(a, j, qv, okv, wv, nullptr, sred, warp, lane);
+  if constexpr (MODE == 1) {
+    basis_dots(a, j, qv, wv, nullptr, sred, warp, lane);
     cta_partials(sred, j + 1, a.part + (long long)blockIdx.x * a.mp1);
   } else {
     float hi = 0.f, lo = 0.f;
@@ -301,7 +339,7 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int 
   if (last_cta(a.counter + t.patch, a.tile_count[t.patch])) {
     const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
     double* T = a.T + (long long)t.patch * a.m * a.m;
-    if (mode == 1) {
+    if constexpr (MODE == 1) {
       for (int i = warp; i <= j; i += kEigWarps) {
         const double s = patch_sum(a.part, tb, tc, a.mp1, i, lane);
         if (lane == 0) {
@@ -325,10 +363,15 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, int 
 }
 
 // -------------------------------------------------------------- restart
-// Vout[:, 0..nk) = V[:, 0..m) Y[:, 0..nk) per pixel, 8 outputs at a time with
-// compensated sums (Y split into FP32 hi + lo), then Vout[nk] = w / beta
+// Vout[:, 0..nk) = V[:, 0..m) Y[:, 0..nk) per pixel, then Vout[nk] = w / beta
 // (restart, Vout is the other basis buffer) -- or, for a converged patch,
-// the nk = nvec Ritz vectors into evec_out.
+// the nk = nvec Ritz vectors into evec_out.  FMA chains over the m basis
+// vectors: the kept vectors come out orthonormal to a few units of
+// rounding, which the next cycle's two CGS passes keep.  A thread takes
+// kRsPix pixels at a time and up to kRsCol outputs per pass over V, so each
+// basis value is loaded once per pass and each 16-byte broadcast of Y
+// (shared memory, zero-padded to kRsCol columns) feeds 4 x kRsPix FMAs.
+constexpr int kRsPix = 2, kRsCol = 32;
 __global__ void __launch_bounds__(kEigThreads) ks_restart(EigArgs a, const float* __restrict__ w,
                                                           float* __restrict__ vout,
                                                           float* __restrict__ evec_out) {
@@ -336,42 +379,67 @@ __global__ void __launch_bounds__(kEigThreads) ks_restart(EigArgs a, const float
   const int mode = a.decision[t.patch];  // 0 idle, 1 restart, 2 final
   if (mode == 0) return;
   const PatchDev P = a.patches[t.patch];
-  const int nk = a.nkeep[t.patch];
-  extern __shared__ float ysh[];  // [m][nk] hi, then lo
-  const double* Y = a.Y + (long long)t.patch * a.m * a.m;
-  for (int idx = threadIdx.x; idx < a.m * nk; idx += blockDim.x) {
-    const int i = idx / nk, c = idx % nk;
-    const double y = Y[i * a.m + c];
-    const float hi = (float)y;
-    ysh[idx] = hi;
-    ysh[a.m * nk + idx] = (float)(y - (double)hi);
-  }
-  __syncthreads();
-  const float inv = (float)(1.0 / sqrt(a.beta2[t.patch]));
-  const long long base = P.vec;
+  const int nk = a.nkeep[t.patch], m = a.m;
+  extern __shared__ float4 ysh4[];  // [m][kRsCol / 4]
+  float* ysh = (float*)ysh4;
+  const double* Y = a.Y + (long long)t.patch * m * m;
+  const int base = (int)P.vec;
   float* out = (mode == 1) ? vout : evec_out;
-  for (int r = 0; r < kEigPix; r++) {
-    const int p = t.p0 + threadIdx.x + r * kEigThreads;
-    if (p >= t.p1) continue;
-    for (int c0 = 0; c0 < nk; c0 += 8) {
-      float hi[8], lo[8];
+  for (int c0 = 0; c0 < nk; c0 += kRsCol) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < m * kRsCol; idx += blockDim.x) {
+      const int i = idx / kRsCol, c = c0 + idx % kRsCol;
+      ysh[idx] = c < nk ? (float)Y[i * m + c] : 0.f;
+    }
+    __syncthreads();
+    for (int r0 = 0; r0 < kEigPix; r0 += kRsPix) {
+      int q[kRsPix];
+      bool ok[kRsPix];
 #pragma unroll
-      for (int c = 0; c < 8; c++) hi[c] = lo[c] = 0.f;
-      for (int i = 0; i < a.m; i++) {
-        const float v = a.V[(long long)i * a.lvec + base + p];
+      for (int k = 0; k < kRsPix; k++) {
+        const int p = t.p0 + threadIdx.x + (r0 + k) * kEigThreads;
+        ok[k] = p < t.p1;
+        q[k] = base + (ok[k] ? p : t.p0);
+      }
+      if (!ok[0]) break;
+      float acc[kRsPix][kRsCol];
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-          if (c0 + c < nk) {
-            ff_add_prod(hi[c], lo[c], ysh[i * nk + c0 + c], v);
-            lo[c] = fmaf(ysh[a.m * nk + i * nk + c0 + c], v, lo[c]);
+      for (int k = 0; k < kRsPix; k++)
+#pragma unroll
+        for (int c = 0; c < kRsCol; c++) acc[k][c] = 0.f;
+#pragma unroll 4
+      for (int i = 0; i < m; i++) {
+        const float* Vi = a.V + (long long)i * a.lvec;
+        float v[kRsPix];
+#pragma unroll
+        for (int k = 0; k < kRsPix; k++) v[k] = Vi[q[k]];
+#pragma unroll
+        for (int c4 = 0; c4 < kRsCol / 4; c4++) {
+          const float4 y = ysh4[i * (kRsCol / 4) + c4];
+#pragma unroll
+          for (int k = 0; k < kRsPix; k++) {
+            acc[k][4 * c4 + 0] = fmaf(y.x, v[k], acc[k][4 * c4 + 0]);
+            acc[k][4 * c4 + 1] = fmaf(y.y, v[k], acc[k][4 * c4 + 1]);
+            acc[k][4 * c4 + 2] = fmaf(y.z, v[k], acc[k][4 * c4 + 2]);
+            acc[k][4 * c4 + 3] = fmaf(y.w, v[k], acc[k][4 * c4 + 3]);
           }
         }
       }
 #pragma unroll
-      for (int c = 0; c < 8; c++)
-        if (c0 + c < nk) out[(long long)(c0 + c) * a.lvec + base + p] = hi[c] + lo[c];
+      for (int k = 0; k < kRsPix; k++) {
+        if (!ok[k]) continue;
+#pragma unroll
+        for (int c = 0; c < kRsCol; c++)
+          if (c0 + c < nk) out[(long long)(c0 + c) * a.lvec + q[k]] = acc[k][c];
+      }
     }
-    if (mode == 1) vout[(long long)nk * a.lvec + base + p] = w[base + p] * inv;
+  }
+  if (mode == 1) {
+    const float inv = (float)(1.0 / sqrt(a.beta2[t.patch]));
+    for (int r = 0; r < kEigPix; r++) {
+      const int p = t.p0 + threadIdx.x + r * kEigThreads;
+      if (p < t.p1) vout[(long long)nk * a.lvec + base + p] = w[base + p] * inv;
+    }
   }
 }
 
@@ -420,12 +488,16 @@ cudaError_t ks_launch_spmv(const EigArgs& a, int ntiles, int j, const float* src
   return cudaGetLastError();
 }
 cudaError_t ks_launch_orth(const EigArgs& a, int ntiles, int j, int mode, float* w, cudaStream_t s) {
-  ks_orth<<<ntiles, kEigThreads, 0, s>>>(a, j, mode, w);
+  if (mode == 1)
+    ks_orth<1><<<ntiles, kEigThreads, 0, s>>>(a, j, w);
+  else
+    ks_orth<2><<<ntiles, kEigThreads, 0, s>>>(a, j, w);
   return cudaGetLastError();
 }
 cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, int max_nk, const float* w, float* vout,
                               float* evec, cudaStream_t s) {
-  ks_restart<<<ntiles, kEigThreads, 2 * a.m * max_nk * sizeof(float), s>>>(a, w, vout, evec);
+  (void)max_nk;
+  ks_restart<<<ntiles, kEigThreads, a.m * kRsCol * sizeof(float), s>>>(a, w, vout, evec);
   return cudaGetLastError();
 }
 
