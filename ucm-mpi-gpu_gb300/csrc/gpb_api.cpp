@@ -731,7 +731,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     es.push_back(grow(b.afull, b.c_afull, (size_t)kFullNC * V));
     es.push_back(grow(b.work_act, b.c_wact, L.work_blk.size()));
     es.push_back(grow(b.berr, b.c_berr, 4));  // error word, spare, block-step queue [2]
-    es.push_back(grow(b.bpart, b.c_bpart, nt * kBlk * kBlk));
+    es.push_back(grow(b.bpart, b.c_bpart, nt * kBlkSplit * kBlk * kBlk));
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
     es.push_back(grow(b.bgram2, b.c_bgram2, np * kBlk * kBlk));
     es.push_back(grow(b.bmat, b.c_bmat, np * kBlk * kBlk));

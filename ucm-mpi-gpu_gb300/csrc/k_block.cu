@@ -189,18 +189,20 @@ __device__ __forceinline__ float f4get(const float4& v) {
 // one staged position (RY, DX) relative to the warp's block origin: the value
 // of this lane's column there, times the coefficient of every block pixel
 // whose stencil covers it
-// C (compensated): products rounded to FP32 are summed as a float-float
-// (TwoSum), removing the accumulation error of the 81-term sum -- the term
-// that dominates near an eigenvector, where the diagonal and the
-// off-diagonal sum nearly cancel; used for the Rayleigh-Ritz products and
-// residuals, not the filter
+// C (compensated): the terms are summed by FMA in groups of four (grp) and
+// each group is folded into a float-float (acc, lo) by an exact TwoSum,
+// which removes the accumulation error of the 81-term sum -- the term that
+// dominates near an eigenvector, where the diagonal and the off-diagonal
+// sum nearly cancel -- down to the groups' own four-term rounding, at about
+// a third of the cost of a TwoSum per term; used for the Rayleigh-Ritz
+// products and residuals, not the filter
 // a half-warp's sub-block: SB_R x SB_C pixels (the two halves of a warp
 // split its 4 x 4 block by rows), two block columns per lane
 constexpr int SB_R = 2, SB_C = 4, SB_N = SB_R * SB_C;
 
 template <class S, bool C, int RY, int DX, int I>
 __device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float2 v, float4 (&cw)[SB_N],
-                                            float2 (&acc)[SB_N], float2 (&lo)[SB_N]) {
+                                            float2 (&acc)[SB_N], float2 (&lo)[SB_N], float2 (&grp)[SB_N]) {
   if constexpr (I < SB_N) {
     constexpr int bi = I / SB_C, bj = I % SB_C;
     if constexpr (S::in(RY - bi, DX - bj)) {
@@ -210,26 +212,32 @@ __device__ __forceinline__ void step_pixels(const float* __restrict__ cs, float2
       if constexpr (idx % 4 == 0) cw[I] = *(const float4*)(cs + (bi * ST_TX + bj) * S::NC + idx);
       const float cf = f4get<idx % 4>(cw[I]);
       if constexpr (C) {
-        float p = __fmul_rn(cf, v.x), s = __fadd_rn(acc[I].x, p), z = s - acc[I].x;
-        lo[I].x += (acc[I].x - (s - z)) + (p - z);
-        acc[I].x = s;
-        p = __fmul_rn(cf, v.y);
-        s = __fadd_rn(acc[I].y, p);
-        z = s - acc[I].y;
-        lo[I].y += (acc[I].y - (s - z)) + (p - z);
-        acc[I].y = s;
+        grp[I].x = fmaf(cf, v.x, grp[I].x);
+        grp[I].y = fmaf(cf, v.y, grp[I].y);
+        // a pixel's offsets run 0 .. N-1 in order: fold after every fourth
+        if constexpr (idx % 4 == 3 || idx == S::N - 1) {
+          float t = acc[I].x + grp[I].x, z = t - acc[I].x;
+          lo[I].x += (acc[I].x - (t - z)) + (grp[I].x - z);
+          acc[I].x = t;
+          t = acc[I].y + grp[I].y;
+          z = t - acc[I].y;
+          lo[I].y += (acc[I].y - (t - z)) + (grp[I].y - z);
+          acc[I].y = t;
+          grp[I] = make_float2(0.f, 0.f);
+        }
       } else {
         acc[I].x = fmaf(cf, v.x, acc[I].x);
         acc[I].y = fmaf(cf, v.y, acc[I].y);
       }
     }
-    step_pixels<S, C, RY, DX, I + 1>(cs, v, cw, acc, lo);
+    step_pixels<S, C, RY, DX, I + 1>(cs, v, cw, acc, lo, grp);
   }
 }
 
 template <class S, bool C, int P>
 __device__ __forceinline__ void step_positions(const float* __restrict__ ys, const float* __restrict__ cs,
-                                               float4 (&cw)[SB_N], float2 (&acc)[SB_N], float2 (&lo)[SB_N]) {
+                                               float4 (&cw)[SB_N], float2 (&acc)[SB_N], float2 (&lo)[SB_N],
+                                               float2 (&grp)[SB_N]) {
   constexpr int NY = SB_R + 2 * S::R, NX = SB_C + 2 * S::R;
   if constexpr (P < NY * NX) {
     constexpr int RY = P / NX - S::R, DX = P % NX - S::R;
@@ -241,9 +249,9 @@ __device__ __forceinline__ void step_positions(const float* __restrict__ ys, con
     }();
     if constexpr (any) {
       const float2 v = *(const float2*)(ys + ((RY + S::R) * StepSmem<S>::PW + (DX + S::R)) * kBlk);
-      step_pixels<S, C, RY, DX, 0>(cs, v, cw, acc, lo);
+      step_pixels<S, C, RY, DX, 0>(cs, v, cw, acc, lo, grp);
     }
-    step_positions<S, C, P + 1>(ys, cs, cw, acc, lo);
+    step_positions<S, C, P + 1>(ys, cs, cw, acc, lo, grp);
   }
 }
 
@@ -395,11 +403,12 @@ __global__ void __launch_bounds__(kStepThreads, 1) cf_step_t(BlkArgs a, const in
         xr[k] = ok ? *(const float2*)(X + (m.vec + (long long)y * m.W + x) * kBlk + col) : make_float2(0.f, 0.f);
       }
     }
-    float2 acc[SB_N], lo[SB_N];
+    float2 acc[SB_N], lo[SB_N], grp[SB_N];
     float4 cw[SB_N];
 #pragma unroll
-    for (int k = 0; k < SB_N; k++) acc[k] = lo[k] = make_float2(0.f, 0.f);
-    step_positions<S, C, 0>(ys + (by * SM::PW + bx) * kBlk + col, cs + (by * ST_TX + bx) * S::NC, cw, acc, lo);
+    for (int k = 0; k < SB_N; k++) acc[k] = lo[k] = grp[k] = make_float2(0.f, 0.f);
+    step_positions<S, C, 0>(ys + (by * SM::PW + bx) * kBlk + col, cs + (by * ST_TX + bx) * S::NC, cw, acc, lo,
+                            grp);
     if constexpr (XS) {
       if (m.cz != 0.f) {
         cp_async_wait_all();
@@ -520,9 +529,58 @@ __device__ __forceinline__ void two_sum_into(float& hi, float& lo, float x) {
   hi = s;
 }
 
+// The reductions and the rotation split each eigensolver tile (kEigTile
+// pixels) into kBlkSplit runs, one CTA each, so a launch has several CTAs
+// per SM and no near-empty last wave.  A CTA's partial sums are float-float
+// pairs in slot blockIdx.x of a.part; the last CTA of a patch adds the
+// slots [tile_begin, tile_begin + tile_count) x kBlkSplit in order, in
+// float-float on the FP32 pipes (one SM adding them in FP64 would take tens
+// of microseconds at GB300's FP64 rate).
+__device__ __forceinline__ void ff2_add(float2& s, float2 b) {
+  const float t = s.x + b.x;
+  const float z = t - s.x;
+  s.y += ((s.x - (t - z)) + (b.x - z)) + b.y;
+  s.x = t;
+}
+struct BlkRun {
+  EigTile t;
+  int p0, p1;
+};
+__device__ __forceinline__ BlkRun blk_run(const BlkArgs& a) {
+  BlkRun r;
+  r.t = a.tiles[blockIdx.x / kBlkSplit];
+  const int len = (r.t.p1 - r.t.p0 + kBlkSplit - 1) / kBlkSplit;
+  r.p0 = min(r.t.p1, r.t.p0 + (int)(blockIdx.x % kBlkSplit) * len);
+  r.p1 = min(r.t.p1, r.p0 + len);
+  return r;
+}
+// true in every thread of the last CTA of patch t.patch to arrive
+__device__ __forceinline__ bool blk_last(const BlkArgs& a, int patch) {
+  __shared__ int is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int prev = atomicAdd(a.counter + patch, 1);
+    is_last = (prev == a.tile_count[patch] * kBlkSplit - 1);
+    if (is_last) a.counter[patch] = 0;
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+// sum of element e over the patch's CTA slots (stride floats2 per slot)
+__device__ __forceinline__ double blk_sum(const BlkArgs& a, int patch, int e, int stride) {
+  const float2* part = (const float2*)a.part;
+  const int b0 = a.tile_begin[patch] * kBlkSplit, b1 = b0 + a.tile_count[patch] * kBlkSplit;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int b = b0; b < b1; b++) ff2_add(acc, part[(long long)b * stride + e]);
+  return (double)acc.x + (double)acc.y;
+}
+
 __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restrict__ U,
                                                const float* __restrict__ V, double* __restrict__ out) {
-  const EigTile t = a.tiles[blockIdx.x];
+  const BlkRun run = blk_run(a);
+  const EigTile t = run.t;
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
   extern __shared__ __align__(16) float gsm[];  // us[GR_CH][32], vs[GR_CH][32]; reused for the group sums
@@ -533,13 +591,13 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
   float hi[16], lo[16];
 #pragma unroll
   for (int k = 0; k < 16; k++) hi[k] = lo[k] = 0.f;
-  for (int p0 = t.p0; p0 < t.p1; p0 += GR_CH) {
+  for (int p0 = run.p0; p0 < run.p1; p0 += GR_CH) {
     __syncthreads();
     for (int f = threadIdx.x; f < GR_CH * kBlk / 4; f += blockDim.x) {
       const int pp = f / (kBlk / 4), c4 = f % (kBlk / 4);
       const int p = p0 + pp;
       float4 u = make_float4(0.f, 0.f, 0.f, 0.f), v = u;
-      if (p < t.p1) {
+      if (p < run.p1) {
         u = ((const float4*)(U + (P.vec + p) * kBlk))[c4];
         v = ((const float4*)(V + (P.vec + p) * kBlk))[c4];
       }
@@ -564,46 +622,36 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
 #pragma unroll
     for (int k = 0; k < 16; k++) two_sum_into(hi[k], lo[k], acc[k]);
   }
-  // the four groups' blocks, summed in FP64
+  // the four groups' blocks, summed in float-float
   __syncthreads();
-  double* red = (double*)gsm;  // [4][32 * 32]
+  float2* red = (float2*)gsm;  // [4][32 * 32]
 #pragma unroll
-  for (int k = 0; k < 16; k++) red[grp * kBlk * kBlk + (i0 + k / 4) * kBlk + j0 + k % 4] = (double)hi[k] + (double)lo[k];
+  for (int k = 0; k < 16; k++) red[grp * kBlk * kBlk + (i0 + k / 4) * kBlk + j0 + k % 4] = make_float2(hi[k], lo[k]);
   __syncthreads();
-  double* part = a.part + (long long)blockIdx.x * kBlk * kBlk;
-  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x)
-    part[e] = red[e] + red[kBlk * kBlk + e] + red[2 * kBlk * kBlk + e] + red[3 * kBlk * kBlk + e];
-  // last CTA of the patch sums the partials
-  __shared__ int is_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const int prev = atomicAdd(a.counter + t.patch, 1);
-    is_last = (prev == a.tile_count[t.patch] - 1);
-    if (is_last) a.counter[t.patch] = 0;
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
+  float2* part = (float2*)a.part + (long long)blockIdx.x * kBlk * kBlk;
   for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) {
-    double s = 0;
-    for (int b = tb; b < tb + tc; b++) s += a.part[(long long)b * kBlk * kBlk + e];
-    out[(long long)t.patch * kBlk * kBlk + e] = s;
+    float2 sum = red[e];
+    for (int g = 1; g < 4; g++) ff2_add(sum, red[g * kBlk * kBlk + e]);
+    part[e] = sum;
   }
+  if (!blk_last(a, t.patch)) return;
+  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x)
+    out[(long long)t.patch * kBlk * kBlk + e] = blk_sum(a, t.patch, e, kBlk * kBlk);
 }
 
 // U <- U M (and V <- V M if V), M = a.mat[patch] (32 x 32, FP64 on the
-// host), one thread per pixel row.  C (the Rayleigh-Ritz rotation): M is
-// split into FP32 hi + lo parts and each output sums its 32 products as a
-// float-float (TwoProduct by FMA, TwoSum), so the Ritz vectors carry no more
-// than FP32 storage rounding; a plain FP32 sum (enough for the
+// host), two pixel rows per thread.  C (the Rayleigh-Ritz rotation): M is
+// split into FP32 hi + lo parts; each output sums its products with hi by
+// FMA in groups of four, folded into a float-float by an exact TwoSum, and
+// its products with lo by FMA into the low word, so the Ritz vectors carry
+// little more than FP32 storage rounding; a plain FP32 sum (enough for the
 // orthonormalisation passes, which the next Rayleigh-Ritz step corrects)
 // leaves ~3e-7 relative error per element.
 template <bool C>
 __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ U, float* __restrict__ V,
                                                  int ncols) {
-  const EigTile t = a.tiles[blockIdx.x];
+  const BlkRun run = blk_run(a);
+  const EigTile t = run.t;
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
   __shared__ __align__(16) float mh[kBlk][kBlk], ml[kBlk][kBlk];
@@ -615,42 +663,68 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
     ml[e / kBlk][e % kBlk] = (float)(m - (double)h);
   }
   __syncthreads();
-  for (int p = t.p0 + threadIdx.x; p < t.p1; p += blockDim.x) {
+  // two pixel rows per thread, so each broadcast load of M feeds both
+  for (int p = run.p0 + threadIdx.x; p < run.p1; p += 2 * blockDim.x) {
+    const bool ok1 = p + (int)blockDim.x < run.p1;
     for (int which = 0; which < (V ? 2 : 1); which++) {
-      float* row = (which ? V : U) + (P.vec + p) * kBlk;
-      float x[kBlk];
+      float* rows[2];
+      rows[0] = (which ? V : U) + (P.vec + p) * kBlk;
+      rows[1] = ok1 ? rows[0] + (long long)blockDim.x * kBlk : rows[0];
+      float x[2][kBlk];
 #pragma unroll
-      for (int c = 0; c < kBlk; c += 4) {
-        const float4 v = *(const float4*)(row + c);
-        x[c] = v.x;
-        x[c + 1] = v.y;
-        x[c + 2] = v.z;
-        x[c + 3] = v.w;
-      }
+      for (int k = 0; k < 2; k++)
+#pragma unroll
+        for (int c = 0; c < kBlk; c += 4) {
+          const float4 v = *(const float4*)(rows[k] + c);
+          x[k][c] = v.x;
+          x[k][c + 1] = v.y;
+          x[k][c + 2] = v.z;
+          x[k][c + 3] = v.w;
+        }
 #pragma unroll 1
       for (int c0 = 0; c0 < kBlk; c0 += 4) {
-        float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+        float hi[2][4], lo[2][4], g[2][4];
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+#pragma unroll
+          for (int j = 0; j < 4; j++) hi[k][j] = lo[k][j] = g[k][j] = 0.f;
 #pragma unroll
         for (int r = 0; r < kBlk; r++) {
           const float4 h4 = *(const float4*)&mh[r][c0];  // broadcast: every thread reads the same row
-          const float4 l4 = *(const float4*)&ml[r][c0];
-          const float hh[4] = {h4.x, h4.y, h4.z, h4.w}, ll[4] = {l4.x, l4.y, l4.z, l4.w};
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            if constexpr (C) {
-              const float pr = __fmul_rn(x[r], hh[j]);  // kept apart from the add below
-              const float pe = fmaf(x[r], hh[j], -pr);  // exact error of the product
-              const float s = __fadd_rn(hi[j], pr);
-              const float z = s - hi[j];
-              lo[j] += ((hi[j] - (s - z)) + (pr - z)) + fmaf(x[r], ll[j], pe);
-              hi[j] = s;
-            } else {
-              hi[j] = fmaf(x[r], hh[j], hi[j]);
-            }
+          const float hh[4] = {h4.x, h4.y, h4.z, h4.w};
+          float ll[4] = {0.f, 0.f, 0.f, 0.f};
+          if constexpr (C) {
+            const float4 l4 = *(const float4*)&ml[r][c0];
+            ll[0] = l4.x;
+            ll[1] = l4.y;
+            ll[2] = l4.z;
+            ll[3] = l4.w;
           }
+#pragma unroll
+          for (int k = 0; k < 2; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              if constexpr (C) {
+                g[k][j] = fmaf(x[k][r], hh[j], g[k][j]);
+                lo[k][j] = fmaf(x[k][r], ll[j], lo[k][j]);
+                if ((r & 3) == 3) {  // r is a compile-time constant here
+                  const float sum = hi[k][j] + g[k][j], z = sum - hi[k][j];
+                  lo[k][j] += (hi[k][j] - (sum - z)) + (g[k][j] - z);
+                  hi[k][j] = sum;
+                  g[k][j] = 0.f;
+                }
+              } else {
+                hi[k][j] = fmaf(x[k][r], hh[j], hi[k][j]);
+              }
+            }
         }
-        if (c0 < ncols)
-          *(float4*)(row + c0) = make_float4(hi[0] + lo[0], hi[1] + lo[1], hi[2] + lo[2], hi[3] + lo[3]);
+        if (c0 < ncols) {
+          *(float4*)(rows[0] + c0) = make_float4(hi[0][0] + lo[0][0], hi[0][1] + lo[0][1], hi[0][2] + lo[0][2],
+                                                 hi[0][3] + lo[0][3]);
+          if (ok1)
+            *(float4*)(rows[1] + c0) = make_float4(hi[1][0] + lo[1][0], hi[1][1] + lo[1][1], hi[1][2] + lo[1][2],
+                                                   hi[1][3] + lo[1][3]);
+        }
       }
     }
   }
@@ -659,42 +733,29 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
 // per-column |A x_c - theta_c x_c|^2 (AX and X given), last CTA sums
 __global__ void __launch_bounds__(256) cf_resid(BlkArgs a, const float* __restrict__ X,
                                                 const float* __restrict__ AX, double* __restrict__ out) {
-  const EigTile t = a.tiles[blockIdx.x];
+  const BlkRun run = blk_run(a);
+  const EigTile t = run.t;
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
   const int c = threadIdx.x & 31, lanegroup = threadIdx.x >> 5;
   const float th = (float)a.theta[(long long)t.patch * kBlk + c];
   float hi = 0.f, lo = 0.f;
-  for (int p = t.p0 + lanegroup; p < t.p1; p += 8) {
+#pragma unroll 4
+  for (int p = run.p0 + lanegroup; p < run.p1; p += 8) {
     const long long q = (P.vec + p) * kBlk + c;
     const float r = fmaf(-th, X[q], AX[q]);
     ffp(hi, lo, r, r);
   }
-  __shared__ double red[8][kBlk];
-  red[lanegroup][c] = (double)hi + (double)lo;
+  __shared__ float2 red[8][kBlk];
+  red[lanegroup][c] = make_float2(hi, lo);
   __syncthreads();
   if (threadIdx.x < kBlk) {
-    double s = 0;
-    for (int g = 0; g < 8; g++) s += red[g][threadIdx.x];
-    a.part[(long long)blockIdx.x * kBlk * kBlk + threadIdx.x] = s;
+    float2 sum = red[0][threadIdx.x];
+    for (int g = 1; g < 8; g++) ff2_add(sum, red[g][threadIdx.x]);
+    ((float2*)a.part)[(long long)blockIdx.x * kBlk + threadIdx.x] = sum;
   }
-  __shared__ int is_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const int prev = atomicAdd(a.counter + t.patch, 1);
-    is_last = (prev == a.tile_count[t.patch] - 1);
-    if (is_last) a.counter[t.patch] = 0;
-  }
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  if (threadIdx.x < kBlk) {
-    const int tb = a.tile_begin[t.patch], tc = a.tile_count[t.patch];
-    double s = 0;
-    for (int b = tb; b < tb + tc; b++) s += a.part[(long long)b * kBlk * kBlk + threadIdx.x];
-    out[(long long)t.patch * kBlk + threadIdx.x] = s;
-  }
+  if (!blk_last(a, t.patch)) return;
+  if (threadIdx.x < kBlk) out[(long long)t.patch * kBlk + threadIdx.x] = blk_sum(a, t.patch, threadIdx.x, kBlk);
 }
 
 // columns 0..nvec-1 of X into separate vectors evec[c][vec layout]
@@ -951,20 +1012,20 @@ cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const f
     cudaFuncSetAttribute(cf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  cf_gram<<<ntiles, 256, smem, s>>>(a, U, V, out);
+  cf_gram<<<ntiles * kBlkSplit, 256, smem, s>>>(a, U, V, out);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,
                              bool comp) {
   if (comp)
-    cf_rotate<true><<<ntiles, 256, 0, s>>>(a, U, V, ncols);
+    cf_rotate<true><<<ntiles * kBlkSplit, 256, 0, s>>>(a, U, V, ncols);
   else
-    cf_rotate<false><<<ntiles, 256, 0, s>>>(a, U, V, ncols);
+    cf_rotate<false><<<ntiles * kBlkSplit, 256, 0, s>>>(a, U, V, ncols);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const float* AX, double* out,
                             cudaStream_t s) {
-  cf_resid<<<ntiles, 256, 0, s>>>(a, X, AX, out);
+  cf_resid<<<ntiles * kBlkSplit, 256, 0, s>>>(a, X, AX, out);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_extract(const BlkArgs& a, int ntiles, const float* X, float* evec, int nvec,

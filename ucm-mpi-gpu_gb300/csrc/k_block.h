@@ -57,6 +57,7 @@ cudaError_t cf_launch_prolong(const CoarseArgs& c, int nwork_f, const float* xc,
 void upload_block(const HostTables& t, cudaStream_t s);
 constexpr int kStepTileH = 8, kStepTileW = 16;  // cf_step tile (work list entries)
 constexpr int kFullNC = 84, kCoarseNC = 52;      // floats per pixel-major stencil row
+constexpr int kBlkSplit = 4;  // CTAs per eigensolver tile in cf_gram / cf_rotate / cf_resid
 // variant (bit-identical results, chosen by the autotuner): bit 0 stages X
 // through shared memory, bit 1 takes tiles from the device work queue
 constexpr int kStepVariants = 4, kStepDefault = 1;  // default (untuned): X staged, static tiles

@@ -370,9 +370,11 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, floa
 // rounding, which the next cycle's two CGS passes keep.  A thread takes
 // kRsPix pixels at a time and up to kRsCol outputs per pass over V, so each
 // basis value is loaded once per pass and each 16-byte broadcast of Y
-// (shared memory, zero-padded to kRsCol columns) feeds 4 x kRsPix FMAs.
-constexpr int kRsPix = 2, kRsCol = 32;
-__global__ void __launch_bounds__(kEigThreads) ks_restart(EigArgs a, const float* __restrict__ w,
+// (shared memory, zero-padded to kRsCol columns) feeds 4 x kRsPix FMAs;
+// one pixel per thread (80 registers) keeps three CTAs on an SM, where two
+// (140 registers) allowed one.
+constexpr int kRsPix = 1, kRsCol = 32;
+__global__ void __launch_bounds__(kEigThreads, 3) ks_restart(EigArgs a, const float* __restrict__ w,
                                                           float* __restrict__ vout,
                                                           float* __restrict__ evec_out) {
   const EigTile t = a.tiles[blockIdx.x];
