@@ -43,9 +43,6 @@ __global__ void __launch_bounds__(1024) k_minmax(const PatchDev* __restrict__ pa
   const int pt = blockIdx.x, i = blockIdx.y;
   const PatchDev P = patches[pt];
   float mn = FLT_MAX, mx = -FLT_MAX;
-  // one CTA per (patch, vector): unrolled so each thread has several
-  // independent load pairs in flight
-#pragma unroll 4
   for (int p = threadIdx.x; p < P.N; p += blockDim.x) {
     const float v = evecs[(long long)i * lvec + P.vec + p] * dis[P.vec + p];
     mn = fminf(mn, v);
