@@ -647,6 +647,16 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
 // little more than FP32 storage rounding; a plain FP32 sum (enough for the
 // orthonormalisation passes, which the next Rayleigh-Ritz step corrects)
 // leaves ~3e-7 relative error per element.
+// Each warp stages its own 64 rows in shared memory -- coalesced 16-byte
+// loads in, the rotation on each lane's two rows there, coalesced stores
+// out -- synchronising only with __syncwarp, so the warps of a CTA overlap
+// their load, compute and store phases.  (Threads loading their own 128-byte
+// rows from global memory made every warp access touch 32 lines; staging
+// behind CTA-wide barriers serialised the phases.)  Row pitch 36 floats: the
+// 8 lanes of a 16-byte access phase reach 8 rows in distinct banks.
+constexpr int RW_ROWS = 64, RW_PITCH = kBlk + 4;
+constexpr int kRotSmem = 8 * RW_ROWS * RW_PITCH * sizeof(float);
+static_assert(8 * RW_ROWS == kEigTile / kBlkSplit, "8 warps x 64 rows cover a CTA's run");
 template <bool C>
 __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ U, float* __restrict__ V,
                                                  int ncols) {
@@ -654,6 +664,7 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
   const EigTile t = run.t;
   if (!a.active[t.patch]) return;
   const PatchDev P = a.patches[t.patch];
+  extern __shared__ __align__(16) float rsm[];  // [8 warps][RW_ROWS][RW_PITCH]
   __shared__ __align__(16) float mh[kBlk][kBlk], ml[kBlk][kBlk];
   const double* M = a.mat + (long long)t.patch * kBlk * kBlk;
   for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) {
@@ -663,13 +674,20 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
     ml[e / kBlk][e % kBlk] = (float)(m - (double)h);
   }
   __syncthreads();
-  // two pixel rows per thread, so each broadcast load of M feeds both
-  for (int p = run.p0 + threadIdx.x; p < run.p1; p += 2 * blockDim.x) {
-    const bool ok1 = p + (int)blockDim.x < run.p1;
-    for (int which = 0; which < (V ? 2 : 1); which++) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wp0 = run.p0 + warp * RW_ROWS;
+  const int n = max(0, min(RW_ROWS, run.p1 - wp0));
+  float* ws = rsm + warp * RW_ROWS * RW_PITCH;
+  for (int which = 0; which < (V ? 2 : 1); which++) {
+    float4* g4 = (float4*)((which ? V : U) + (P.vec + wp0) * kBlk);
+    for (int f = lane; f < n * (kBlk / 4); f += 32) *(float4*)(ws + (f >> 3) * RW_PITCH + (f & 7) * 4) = g4[f];
+    __syncwarp();
+    // two rows per lane, so each broadcast load of M feeds both
+    if (lane < n) {
+      const bool ok1 = lane + 32 < n;
       float* rows[2];
-      rows[0] = (which ? V : U) + (P.vec + p) * kBlk;
-      rows[1] = ok1 ? rows[0] + (long long)blockDim.x * kBlk : rows[0];
+      rows[0] = ws + lane * RW_PITCH;
+      rows[1] = ok1 ? rows[0] + 32 * RW_PITCH : rows[0];
       float x[2][kBlk];
 #pragma unroll
       for (int k = 0; k < 2; k++)
@@ -727,6 +745,9 @@ __global__ void __launch_bounds__(256) cf_rotate(BlkArgs a, float* __restrict__ 
         }
       }
     }
+    __syncwarp();
+    for (int f = lane; f < n * (kBlk / 4); f += 32) g4[f] = *(const float4*)(ws + (f >> 3) * RW_PITCH + (f & 7) * 4);
+    __syncwarp();
   }
 }
 
@@ -1017,10 +1038,16 @@ cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const f
 }
 cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,
                              bool comp) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(cf_rotate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRotSmem);
+    cudaFuncSetAttribute(cf_rotate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRotSmem);
+    attr = true;
+  }
   if (comp)
-    cf_rotate<true><<<ntiles * kBlkSplit, 256, 0, s>>>(a, U, V, ncols);
+    cf_rotate<true><<<ntiles * kBlkSplit, 256, kRotSmem, s>>>(a, U, V, ncols);
   else
-    cf_rotate<false><<<ntiles * kBlkSplit, 256, 0, s>>>(a, U, V, ncols);
+    cf_rotate<false><<<ntiles * kBlkSplit, 256, kRotSmem, s>>>(a, U, V, ncols);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const float* AX, double* out,
