@@ -153,10 +153,10 @@ def test_trained_start_on_held_out_patches(orc):
     of 256^2 labelled by the plain solver, 60 epochs) on 8 held-out 512^2
     patches.  At the workload's evaluation residual (1e-4, gap rule off) the
     block solver started from the network needs fewer matvecs than from a
-    random block (measured over 32 such patches: 6,740 vs 7,127 per patch,
-    11.2 vs 11.6 ms).  At the library's tolerance (1e-6, which gPb within
+    random block (measured over 200 such patches: 6,816 vs 7,084 per patch,
+    11.2 vs 11.5 ms).  At the library's tolerance (1e-6, which gPb within
     1e-3 needs) it converges to the same residual bound and gPb within 1e-3
-    of the oracle; there the start's advantage is gone (62.3 vs 61.6 ms)."""
+    of the oracle; there the start's advantage is gone (54.7 vs 54.8 ms)."""
     import gpb
     from gpb import learned
     w = np.load(learned.WEIGHTS)
