@@ -10,7 +10,7 @@
 //              recurrence, Zhou & Saad 2007; with alpha=1, beta=gamma=0 it
 //              is the plain block SpMV)
 //   cf_gram    G = U^T V per patch (32 x 32), FP32 FMA runs folded into
-//              float-float sums, FP64 cross-CTA sums by the last CTA
+//              float-float sums, summed across CTAs by the patch's last CTA
 //   cf_rotate  U <- U M (32 x 32 per patch), optionally V <- V M too
 //   cf_resid   |A x_c - theta_c x_c|^2 per column
 //   cf_extract the first nvec columns into separate vectors (sPb layout)
