@@ -19,3 +19,4 @@ def test_autotuner_bookkeeping(tmp_path):
                     os.path.join(ROOT, "tests", "autotune_check.cpp"), "-o", exe], check=True)
     out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0 and "ok" in out.stdout, out.stdout + out.stderr
+

@@ -37,6 +37,8 @@
 
 namespace gpb {
 void sym_eig(double* A, int n, double* w, double* Z);
+void lowdin(const double* G, int n, double* M);
+void mat_mul(const double* A, const double* B, double* C, int n, bool at);
 }
 
 using namespace gpb;
@@ -963,22 +965,6 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
 // Gram matrix (symmetric orthonormalisation, FP64 on the host) and performs a
 // Rayleigh-Ritz step; the host solves the 32 x 32 problems.  The start block
 // is the warm start; without one it is seeded noise.
-static void lowdin(const double* G, int n, double* M) {
-  // M = G^-1/2 (eigenvalues clamped), so that U M has orthonormal columns
-  std::vector<double> A(G, G + (size_t)n * n), w(n), Z((size_t)n * n), sq(n);
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) A[i * n + j] = 0.5 * (G[i * n + j] + G[j * n + i]);
-  gpb::sym_eig(A.data(), n, w.data(), Z.data());
-  const double floor_ = std::max(w[n - 1], 1e-300) * 1e-15;
-  for (int k = 0; k < n; k++) sq[k] = sqrt(std::max(w[k], floor_));
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < n; j++) {
-      double v = 0;
-      for (int k = 0; k < n; k++) v += Z[i * n + k] * Z[j * n + k] / sq[k];
-      M[i * n + j] = v;
-    }
-}
-
 // one level of the block solver: its layout, device tables, operator and
 // the four block buffers
 struct Level {
@@ -1110,7 +1096,7 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     CK(cudaStreamSynchronize(s));
     ctx->tuner.collect();
     ctx->host_pool().run(np, [&](int i) {
-      if (active[i]) lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
+      if (active[i]) gpb::lowdin(G.data() + i * BB, kBlk, M.data() + i * BB);
     });
     if (ctx->trace && active[0])
       fprintf(stderr, "[gpb] gram patch 0: G00 %.3e G11 %.3e G3131 %.3e M00 %.3e\n", G[0], G[kBlk + 1], G[BB - 1],
@@ -1130,32 +1116,17 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
       mv[i] += kBlk;
       // M1 = G2^-1/2; the Ritz pairs of M1 H M1 give the rotation M1 Z
       std::vector<double> M1(BB), Hs(BB), T(BB), C(BB), w(kBlk), Zm(BB);
-      lowdin(G2.data() + i * BB, kBlk, M1.data());
+      gpb::lowdin(G2.data() + i * BB, kBlk, M1.data());
       for (int r = 0; r < kBlk; r++)
         for (int c = 0; c < kBlk; c++)
           Hs[r * kBlk + c] = 0.5 * (G[i * BB + r * kBlk + c] + G[i * BB + c * kBlk + r]);
-      for (int r = 0; r < kBlk; r++)
-        for (int c = 0; c < kBlk; c++) {
-          double v = 0;
-          for (int k = 0; k < kBlk; k++) v += Hs[r * kBlk + k] * M1[k * kBlk + c];
-          T[r * kBlk + c] = v;
-        }
-      for (int r = 0; r < kBlk; r++)
-        for (int c = 0; c < kBlk; c++) {
-          double v = 0;
-          for (int k = 0; k < kBlk; k++) v += M1[k * kBlk + r] * T[k * kBlk + c];
-          C[r * kBlk + c] = v;
-        }
+      gpb::mat_mul(Hs.data(), M1.data(), T.data(), kBlk, false);  // T = Hs M1
+      gpb::mat_mul(M1.data(), T.data(), C.data(), kBlk, true);    // C = M1^T T
       for (int r = 0; r < kBlk; r++)
         for (int c = r + 1; c < kBlk; c++) C[r * kBlk + c] = C[c * kBlk + r] = 0.5 * (C[r * kBlk + c] + C[c * kBlk + r]);
       gpb::sym_eig(C.data(), kBlk, w.data(), Zm.data());
       for (int c = 0; c < kBlk; c++) theta[(size_t)i * kBlk + c] = w[c];
-      for (int r = 0; r < kBlk; r++)
-        for (int c = 0; c < kBlk; c++) {
-          double v = 0;
-          for (int k = 0; k < kBlk; k++) v += M1[r * kBlk + k] * Zm[k * kBlk + c];
-          M[i * BB + r * kBlk + c] = v;
-        }
+      gpb::mat_mul(M1.data(), Zm.data(), M.data() + i * BB, kBlk, false);  // M = M1 Zm
     });
     CK(cudaMemcpyAsync(b.bmat, M.data(), np * BB * sizeof(double), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.btheta, theta.data(), theta.size() * sizeof(double), cudaMemcpyHostToDevice, s));

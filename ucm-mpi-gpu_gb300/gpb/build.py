@@ -17,6 +17,9 @@ LIB = os.path.join(PKG, "libgpb.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
           "-I" + CSRC, "-I" + os.path.join(os.path.dirname(ROOT), "include")]
+# host code whose loops the compiler should vectorise (results are the same
+# to the bit: -ffp-contract=off and no reassociation)
+HOST_O3 = {"eig_host.cpp"}
 SOURCES = ["tables.cpp", "eig_host.cpp", "gpb_api.cpp", "gpb_damascene.cpp", "io_writers.cpp", "k_block.cu",
            "k_front.cu", "k_static.cu", "k_stitch.cu", "k_spfeat.cu", "k_cues.cu", "k_buildw.cu", "k_eig.cu", "k_spb.cu",
            "ucm_host.cpp", "ucm_api.cpp", "k_ucm.cu", "k_warmnet.cu", "k_learned.cu"]
@@ -38,6 +41,8 @@ def _compile(src):
     if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
         return out
     cmd = [nvcc()] + ARCH + COMMON + ["-c", path, "-o", out]
+    if src in HOST_O3:
+        cmd += ["-Xcompiler", "-O3"]
     if src.endswith(".cu"):
         cmd += ["-Xptxas", "-warn-spills"]
     r = subprocess.run(cmd, capture_output=True, text=True)
