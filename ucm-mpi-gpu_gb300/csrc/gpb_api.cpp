@@ -733,7 +733,7 @@ static gpb_status ensure_buffers(gpb_ctx* ctx, const Layout& L, bool layout_chan
     es.push_back(grow(b.afull, b.c_afull, (size_t)kFullNC * V));
     es.push_back(grow(b.work_act, b.c_wact, L.work_blk.size()));
     es.push_back(grow(b.berr, b.c_berr, 4));  // error word, spare, block-step queue [2]
-    es.push_back(grow(b.bpart, b.c_bpart, nt * kBlkSplit * kBlk * kBlk));
+    es.push_back(grow(b.bpart, b.c_bpart, nt * kBlkSplit * 2 * kBlk * kBlk));  // two Gram matrices per slot
     es.push_back(grow(b.bgram, b.c_bgram, np * kBlk * kBlk));
     es.push_back(grow(b.bgram2, b.c_bgram2, np * kBlk * kBlk));
     es.push_back(grow(b.bmat, b.c_bmat, np * kBlk * kBlk));
@@ -1105,12 +1105,11 @@ static gpb_status solve_block(gpb_ctx* ctx, const Level& lv, bool have_start, do
     CK(cf_launch_rotate(a, nt, F, nullptr, kBlk, s));
     CK(upload_unit());
     CK(cf_launch_step(a, work_blk, nwb, F, F, AF, 0, s, comp, step_variant(nwb)));
-    CK(cf_launch_gram(a, nt, F, F, b.bgram2, s));
-    CK(cf_launch_gram(a, nt, F, AF, b.bgram, s));
+    CK(cf_launch_gram(a, nt, F, AF, b.bgram, s, b.bgram2));  // G = F^T AF and G2 = F^T F in one pass
     CK(cudaMemcpyAsync(G2.data(), b.bgram2, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(G.data(), b.bgram, np * BB * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    ctx->launches += 5;
+    ctx->launches += 4;
     ctx->host_pool().run(np, [&](int i) {
       if (!active[i]) return;
       mv[i] += kBlk;

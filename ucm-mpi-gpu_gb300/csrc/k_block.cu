@@ -577,8 +577,13 @@ __device__ __forceinline__ double blk_sum(const BlkArgs& a, int patch, int e, in
   return (double)acc.x + (double)acc.y;
 }
 
-__global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restrict__ U,
-                                               const float* __restrict__ V, double* __restrict__ out) {
+// TWO: one pass computes out = U^T V and out2 = U^T U (the Rayleigh-Ritz
+// step's two Gram matrices), each element with the same operations in the
+// same order as a pass of its own, so the results are the same to the bit.
+template <bool TWO>
+__global__ void __launch_bounds__(256, TWO ? 2 : 3) cf_gram(BlkArgs a, const float* __restrict__ U,
+                                                            const float* __restrict__ V, double* __restrict__ out,
+                                                            double* __restrict__ out2) {
   const BlkRun run = blk_run(a);
   const EigTile t = run.t;
   if (!a.active[t.patch]) return;
@@ -588,9 +593,12 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
   float* vs = gsm + GR_CH * kBlk;
   const int grp = threadIdx.x >> 6, lt = threadIdx.x & 63;
   const int i0 = (lt >> 3) * 4, j0 = (lt & 7) * 4;
-  float hi[16], lo[16];
+  constexpr int NG = TWO ? 2 : 1;  // Gram matrices formed
+  float hi[NG][16], lo[NG][16];
 #pragma unroll
-  for (int k = 0; k < 16; k++) hi[k] = lo[k] = 0.f;
+  for (int g = 0; g < NG; g++)
+#pragma unroll
+    for (int k = 0; k < 16; k++) hi[g][k] = lo[g][k] = 0.f;
   for (int p0 = run.p0; p0 < run.p1; p0 += GR_CH) {
     __syncthreads();
     for (int f = threadIdx.x; f < GR_CH * kBlk / 4; f += blockDim.x) {
@@ -605,11 +613,13 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
       ((float4*)vs)[f] = v;
     }
     __syncthreads();
-    float acc[16];
+    float acc[NG][16];
 #pragma unroll
-    for (int k = 0; k < 16; k++) acc[k] = 0.f;
+    for (int g = 0; g < NG; g++)
+#pragma unroll
+      for (int k = 0; k < 16; k++) acc[g][k] = 0.f;
     const int pbeg = grp * (GR_CH / 4);
-#pragma unroll 4
+#pragma unroll(TWO ? 2 : 4)
     for (int pp = pbeg; pp < pbeg + GR_CH / 4; pp++) {
       const float4 u4 = *(const float4*)(us + pp * kBlk + i0);
       const float4 v4 = *(const float4*)(vs + pp * kBlk + j0);
@@ -617,26 +627,42 @@ __global__ void __launch_bounds__(256) cf_gram(BlkArgs a, const float* __restric
 #pragma unroll
       for (int r = 0; r < 4; r++)
 #pragma unroll
-        for (int c = 0; c < 4; c++) acc[r * 4 + c] = fmaf(uu[r], vv[c], acc[r * 4 + c]);
+        for (int c = 0; c < 4; c++) acc[0][r * 4 + c] = fmaf(uu[r], vv[c], acc[0][r * 4 + c]);
+      if constexpr (TWO) {
+        const float4 w4 = *(const float4*)(us + pp * kBlk + j0);
+        const float ww[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) acc[NG - 1][r * 4 + c] = fmaf(uu[r], ww[c], acc[NG - 1][r * 4 + c]);
+      }
     }
 #pragma unroll
-    for (int k = 0; k < 16; k++) two_sum_into(hi[k], lo[k], acc[k]);
+    for (int g = 0; g < NG; g++)
+#pragma unroll
+      for (int k = 0; k < 16; k++) two_sum_into(hi[g][k], lo[g][k], acc[g][k]);
   }
   // the four groups' blocks, summed in float-float
   __syncthreads();
-  float2* red = (float2*)gsm;  // [4][32 * 32]
+  float2* red = (float2*)gsm;  // [NG][4][32 * 32] (64 KB for two)
 #pragma unroll
-  for (int k = 0; k < 16; k++) red[grp * kBlk * kBlk + (i0 + k / 4) * kBlk + j0 + k % 4] = make_float2(hi[k], lo[k]);
+  for (int g = 0; g < NG; g++)
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+      red[(g * 4 + grp) * kBlk * kBlk + (i0 + k / 4) * kBlk + j0 + k % 4] = make_float2(hi[g][k], lo[g][k]);
   __syncthreads();
-  float2* part = (float2*)a.part + (long long)blockIdx.x * kBlk * kBlk;
-  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x) {
-    float2 sum = red[e];
-    for (int g = 1; g < 4; g++) ff2_add(sum, red[g * kBlk * kBlk + e]);
+  float2* part = (float2*)a.part + (long long)blockIdx.x * NG * kBlk * kBlk;
+  for (int e = threadIdx.x; e < NG * kBlk * kBlk; e += blockDim.x) {
+    const int g = e / (kBlk * kBlk), el = e % (kBlk * kBlk);
+    float2 sum = red[g * 4 * kBlk * kBlk + el];
+    for (int q = 1; q < 4; q++) ff2_add(sum, red[(g * 4 + q) * kBlk * kBlk + el]);
     part[e] = sum;
   }
   if (!blk_last(a, t.patch)) return;
-  for (int e = threadIdx.x; e < kBlk * kBlk; e += blockDim.x)
-    out[(long long)t.patch * kBlk * kBlk + e] = blk_sum(a, t.patch, e, kBlk * kBlk);
+  for (int e = threadIdx.x; e < NG * kBlk * kBlk; e += blockDim.x) {
+    const int g = e / (kBlk * kBlk), el = e % (kBlk * kBlk);
+    (g ? out2 : out)[(long long)t.patch * kBlk * kBlk + el] = blk_sum(a, t.patch, e, NG * kBlk * kBlk);
+  }
 }
 
 // U <- U M (and V <- V M if V), M = a.mat[patch] (32 x 32, FP64 on the
@@ -1026,14 +1052,18 @@ cudaError_t cf_launch_full(const PatchDev* patches, const int4* work16, int nwor
   return cudaGetLastError();
 }
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
-                           cudaStream_t s) {
-  constexpr int smem = 2 * GR_CH * kBlk * sizeof(float);  // 64 KB; the FP64 group sums (32 KB) reuse it
+                           cudaStream_t s, double* out2) {
+  constexpr int smem = 2 * GR_CH * kBlk * sizeof(float);  // 64 KB; the group sums (32 or 64 KB) reuse it
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(cf_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(cf_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(cf_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  cf_gram<<<ntiles * kBlkSplit, 256, smem, s>>>(a, U, V, out);
+  if (out2)
+    cf_gram<true><<<ntiles * kBlkSplit, 256, smem, s>>>(a, U, V, out, out2);
+  else
+    cf_gram<false><<<ntiles * kBlkSplit, 256, smem, s>>>(a, U, V, out, nullptr);
   return cudaGetLastError();
 }
 cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,

@@ -63,8 +63,9 @@ constexpr int kBlkSplit = 4;  // CTAs per eigensolver tile in cf_gram / cf_rotat
 constexpr int kStepVariants = 4, kStepDefault = 1;  // default (untuned): X staged, static tiles
 cudaError_t cf_launch_step(const BlkArgs& a, const int4* work, int nwork, const float* Y, const float* X, float* out,
                            int step, cudaStream_t s, bool comp = false, int variant = kStepDefault);
+// out = U^T V per patch; with out2, out2 = U^T U in the same pass
 cudaError_t cf_launch_gram(const BlkArgs& a, int ntiles, const float* U, const float* V, double* out,
-                           cudaStream_t s);
+                           cudaStream_t s, double* out2 = nullptr);
 cudaError_t cf_launch_rotate(const BlkArgs& a, int ntiles, float* U, float* V, int ncols, cudaStream_t s,
                              bool comp = false);
 cudaError_t cf_launch_resid(const BlkArgs& a, int ntiles, const float* X, const float* AX, double* out,
