@@ -403,7 +403,8 @@ def run_gpu(args):
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_step, "step_ms": [round(t, 3) for t in times],
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "eig": "block Chebyshev-filtered subspace iteration (32 vectors, degree %d) warm-started "
