@@ -931,8 +931,9 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
     CK(cudaMemcpyAsync(b.nkeep, nkeep.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     a.V = Vc;
-    CK(ks_launch_restart(a, nt, std::max(keep, nev), cur, Va, b.evec, s));
-    ctx->launches++;
+    const bool any_final = std::count(decision.begin(), decision.end(), 2) > 0;
+    CK(ks_launch_restart(a, nt, std::max(keep, nev), cur, Va, b.evec, s, any_restart, any_final));
+    ctx->launches += (int)any_restart + (int)any_final;
     std::swap(Vc, Va);
     std::fill(decision.begin(), decision.end(), 0);
     CK(cudaMemcpyAsync(b.decision, decision.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));

@@ -364,79 +364,81 @@ __global__ void __launch_bounds__(kEigThreads, 2) ks_orth(EigArgs a, int j, floa
 
 // -------------------------------------------------------------- restart
 // Vout[:, 0..nk) = V[:, 0..m) Y[:, 0..nk) per pixel, then Vout[nk] = w / beta
-// (restart, Vout is the other basis buffer) -- or, for a converged patch,
-// the nk = nvec Ritz vectors into evec_out.  FMA chains over the m basis
-// vectors: the kept vectors come out orthonormal to a few units of
-// rounding, which the next cycle's two CGS passes keep.  A thread takes
-// kRsPix pixels at a time and up to kRsCol outputs per pass over V, so each
-// basis value is loaded once per pass and each 16-byte broadcast of Y
-// (shared memory, zero-padded to kRsCol columns) feeds 4 x kRsPix FMAs;
-// one pixel per thread (80 registers) keeps three CTAs on an SM, where two
-// (140 registers) allowed one.
-constexpr int kRsPix = 1, kRsCol = 32;
-__global__ void __launch_bounds__(kEigThreads, 3) ks_restart(EigArgs a, const float* __restrict__ w,
-                                                          float* __restrict__ vout,
-                                                          float* __restrict__ evec_out) {
+// (restart, Vout is the other basis buffer) -- or, for a converged patch
+// (FINAL), the nk = nvec Ritz vectors into evec_out.
+// Restart: FMA chains over the m basis vectors; the kept vectors come out
+// orthonormal to a few units of rounding, which the next cycle's two CGS
+// passes keep.  A thread takes one pixel and up to 32 outputs per pass over
+// V, so each basis value is loaded once per pass and each 16-byte broadcast
+// of Y (shared memory, zero-padded) feeds 4 FMAs; 80 registers keep three
+// CTAs on an SM.
+// FINAL: the eigenvectors themselves, where an FMA chain's rounding (about
+// sqrt(m) units) would show in their residual: Y is split into FP32 hi + lo,
+// the hi products are summed by FMA in groups of four folded into a
+// float-float by TwoSum, the lo products into the low word.
+template <bool FINAL>
+__global__ void __launch_bounds__(kEigThreads, 2) ks_restart(EigArgs a, const float* __restrict__ w,
+                                                            float* __restrict__ vout,
+                                                            float* __restrict__ evec_out) {
+  constexpr int COLS = 16;  // outputs per pass over V
   const EigTile t = a.tiles[blockIdx.x];
   const int mode = a.decision[t.patch];  // 0 idle, 1 restart, 2 final
-  if (mode == 0) return;
+  if (mode != (FINAL ? 2 : 1)) return;
   const PatchDev P = a.patches[t.patch];
   const int nk = a.nkeep[t.patch], m = a.m;
-  extern __shared__ float4 ysh4[];  // [m][kRsCol / 4]
+  extern __shared__ float4 ysh4[];  // [m][COLS / 4] hi, then (FINAL) lo
   float* ysh = (float*)ysh4;
   const double* Y = a.Y + (long long)t.patch * m * m;
   const int base = (int)P.vec;
-  float* out = (mode == 1) ? vout : evec_out;
-  for (int c0 = 0; c0 < nk; c0 += kRsCol) {
+  float* out = FINAL ? evec_out : vout;
+  for (int c0 = 0; c0 < nk; c0 += COLS) {
     __syncthreads();
-    for (int idx = threadIdx.x; idx < m * kRsCol; idx += blockDim.x) {
-      const int i = idx / kRsCol, c = c0 + idx % kRsCol;
-      ysh[idx] = c < nk ? (float)Y[i * m + c] : 0.f;
+    for (int idx = threadIdx.x; idx < m * COLS; idx += blockDim.x) {
+      const int i = idx / COLS, c = c0 + idx % COLS;
+      const double y = c < nk ? Y[i * m + c] : 0.0;
+      const float yh = (float)y;
+      ysh[idx] = yh;
+      ysh[m * COLS + idx] = (float)(y - (double)yh);
     }
     __syncthreads();
-    for (int r0 = 0; r0 < kEigPix; r0 += kRsPix) {
-      int q[kRsPix];
-      bool ok[kRsPix];
+    for (int r = 0; r < kEigPix; r++) {
+      const int p = t.p0 + threadIdx.x + r * kEigThreads;
+      if (p >= t.p1) break;
+      const int q = base + p;
+      float acc[COLS], lo[COLS], g[COLS];
 #pragma unroll
-      for (int k = 0; k < kRsPix; k++) {
-        const int p = t.p0 + threadIdx.x + (r0 + k) * kEigThreads;
-        ok[k] = p < t.p1;
-        q[k] = base + (ok[k] ? p : t.p0);
-      }
-      if (!ok[0]) break;
-      float acc[kRsPix][kRsCol];
-#pragma unroll
-      for (int k = 0; k < kRsPix; k++)
-#pragma unroll
-        for (int c = 0; c < kRsCol; c++) acc[k][c] = 0.f;
+      for (int c = 0; c < COLS; c++) acc[c] = lo[c] = g[c] = 0.f;
 #pragma unroll 4
       for (int i = 0; i < m; i++) {
-        const float* Vi = a.V + (long long)i * a.lvec;
-        float v[kRsPix];
+        const float v = a.V[(long long)i * a.lvec + q];
 #pragma unroll
-        for (int k = 0; k < kRsPix; k++) v[k] = Vi[q[k]];
+        for (int c4 = 0; c4 < COLS / 4; c4++) {
+          const float4 y = ysh4[i * (COLS / 4) + c4];
+          const float yv[4] = {y.x, y.y, y.z, y.w};
+          const float4 yl = ysh4[(m + i) * (COLS / 4) + c4];
+          const float ylv[4] = {yl.x, yl.y, yl.z, yl.w};
 #pragma unroll
-        for (int c4 = 0; c4 < kRsCol / 4; c4++) {
-          const float4 y = ysh4[i * (kRsCol / 4) + c4];
+          for (int j = 0; j < 4; j++) {
+            g[4 * c4 + j] = fmaf(yv[j], v, g[4 * c4 + j]);
+            lo[4 * c4 + j] = fmaf(ylv[j], v, lo[4 * c4 + j]);
+          }
+        }
+        if ((i & 3) == 3 || i == m - 1) {
 #pragma unroll
-          for (int k = 0; k < kRsPix; k++) {
-            acc[k][4 * c4 + 0] = fmaf(y.x, v[k], acc[k][4 * c4 + 0]);
-            acc[k][4 * c4 + 1] = fmaf(y.y, v[k], acc[k][4 * c4 + 1]);
-            acc[k][4 * c4 + 2] = fmaf(y.z, v[k], acc[k][4 * c4 + 2]);
-            acc[k][4 * c4 + 3] = fmaf(y.w, v[k], acc[k][4 * c4 + 3]);
+          for (int c = 0; c < COLS; c++) {
+            const float sum = acc[c] + g[c], z = sum - acc[c];
+            lo[c] += (acc[c] - (sum - z)) + (g[c] - z);
+            acc[c] = sum;
+            g[c] = 0.f;
           }
         }
       }
 #pragma unroll
-      for (int k = 0; k < kRsPix; k++) {
-        if (!ok[k]) continue;
-#pragma unroll
-        for (int c = 0; c < kRsCol; c++)
-          if (c0 + c < nk) out[(long long)(c0 + c) * a.lvec + q[k]] = acc[k][c];
-      }
+      for (int c = 0; c < COLS; c++)
+        if (c0 + c < nk) out[(long long)(c0 + c) * a.lvec + q] = acc[c] + lo[c];
     }
   }
-  if (mode == 1) {
+  if constexpr (!FINAL) {
     const float inv = (float)(1.0 / sqrt(a.beta2[t.patch]));
     for (int r = 0; r < kEigPix; r++) {
       const int p = t.p0 + threadIdx.x + r * kEigThreads;
@@ -497,9 +499,10 @@ cudaError_t ks_launch_orth(const EigArgs& a, int ntiles, int j, int mode, float*
   return cudaGetLastError();
 }
 cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, int max_nk, const float* w, float* vout,
-                              float* evec, cudaStream_t s) {
+                              float* evec, cudaStream_t s, bool any_restart, bool any_final) {
   (void)max_nk;
-  ks_restart<<<ntiles, kEigThreads, a.m * kRsCol * sizeof(float), s>>>(a, w, vout, evec);
+  if (any_restart) ks_restart<false><<<ntiles, kEigThreads, 2 * a.m * 16 * sizeof(float), s>>>(a, w, vout, evec);
+  if (any_final) ks_restart<true><<<ntiles, kEigThreads, 2 * a.m * 16 * sizeof(float), s>>>(a, w, vout, evec);
   return cudaGetLastError();
 }
 
