@@ -932,7 +932,7 @@ static gpb_status solve_lanczos(gpb_ctx* ctx, const Layout& L) {
     CK(cudaMemcpyAsync(b.active, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     a.V = Vc;
     const bool any_final = std::count(decision.begin(), decision.end(), 2) > 0;
-    CK(ks_launch_restart(a, nt, std::max(keep, nev), cur, Va, b.evec, s, any_restart, any_final));
+    CK(ks_launch_restart(a, nt, cur, Va, b.evec, s, any_restart, any_final));
     ctx->launches += (int)any_restart + (int)any_final;
     std::swap(Vc, Va);
     std::fill(decision.begin(), decision.end(), 0);

@@ -498,9 +498,8 @@ cudaError_t ks_launch_orth(const EigArgs& a, int ntiles, int j, int mode, float*
     ks_orth<2><<<ntiles, kEigThreads, 0, s>>>(a, j, w);
   return cudaGetLastError();
 }
-cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, int max_nk, const float* w, float* vout,
-                              float* evec, cudaStream_t s, bool any_restart, bool any_final) {
-  (void)max_nk;
+cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, const float* w, float* vout, float* evec,
+                              cudaStream_t s, bool any_restart, bool any_final) {
   if (any_restart) ks_restart<false><<<ntiles, kEigThreads, 2 * a.m * 16 * sizeof(float), s>>>(a, w, vout, evec);
   if (any_final) ks_restart<true><<<ntiles, kEigThreads, 2 * a.m * 16 * sizeof(float), s>>>(a, w, vout, evec);
   return cudaGetLastError();

@@ -46,7 +46,7 @@ cudaError_t ks_launch_spmv(const EigArgs& a, int ntiles, int j, const float* src
 cudaError_t ks_launch_orth(const EigArgs& a, int ntiles, int j, int mode, float* w, cudaStream_t s);
 // the restart of the patches whose decision is 1 and the final Ritz vectors
 // of those whose decision is 2 (each launched only when some patch needs it)
-cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, int max_nk, const float* w, float* vout,
-                              float* evec, cudaStream_t s, bool any_restart, bool any_final);
+cudaError_t ks_launch_restart(const EigArgs& a, int ntiles, const float* w, float* vout, float* evec,
+                              cudaStream_t s, bool any_restart, bool any_final);
 
 }  // namespace gpb
